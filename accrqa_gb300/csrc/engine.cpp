@@ -1,0 +1,679 @@
+// engine.cpp -- host side of the GB300 RQA engine (see engine.hpp).
+#include "engine.hpp"
+
+#include <cfloat>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <memory>
+
+namespace accrqa {
+
+// ===========================================================================
+// Errors
+// ===========================================================================
+static thread_local char g_last_error[512];
+
+void set_last_error(const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_last_error, sizeof(g_last_error), fmt, ap);
+    va_end(ap);
+}
+
+const char *last_error() { return g_last_error; }
+
+Accrqa_Error cuda_error(cudaError_t e, const char *what) {
+    set_last_error("%s: %s", what, cudaGetErrorString(e));
+    if (e == cudaErrorMemoryAllocation) return ERR_CUDA_NOT_ENOUGH_MEMORY;
+    if (e == cudaErrorNoDevice || e == cudaErrorInvalidDevice ||
+        e == cudaErrorInsufficientDriver)
+        return ERR_CUDA_DEVICE_NOT_FOUND;
+    return ERR_CUDA;
+}
+
+#define CU(call, what)                                     \
+    do {                                                   \
+        cudaError_t e_ = (call);                           \
+        if (e_ != cudaSuccess) return cuda_error(e_, what); \
+    } while (0)
+
+// ===========================================================================
+// Device memory and contexts
+// ===========================================================================
+cudaError_t DeviceBuffer::reserve(size_t need) {
+    if (need <= bytes && ptr) return cudaSuccess;
+    release();
+    size_t grow = need + need / 4 + 4096;
+    cudaError_t e = cudaMalloc(&ptr, grow);
+    if (e != cudaSuccess) {
+        ptr = nullptr;
+        bytes = 0;
+        cudaGetLastError();
+        e = cudaMalloc(&ptr, need);   // retry without headroom
+        if (e != cudaSuccess) {
+            ptr = nullptr;
+            return e;
+        }
+        bytes = need;
+        return cudaSuccess;
+    }
+    bytes = grow;
+    return cudaSuccess;
+}
+
+void DeviceBuffer::release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+}
+
+static std::mutex g_ctx_mu;
+static Context *g_ctx[64];
+
+Context *current_context(Accrqa_Error *err) {
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count <= 0) {
+        cudaGetLastError();
+        set_last_error("no CUDA device available (%s)",
+                       e != cudaSuccess ? cudaGetErrorString(e) : "count = 0");
+        *err = ERR_CUDA_DEVICE_NOT_FOUND;
+        return nullptr;
+    }
+    int dev = 0;
+    e = cudaGetDevice(&dev);
+    if (e != cudaSuccess || dev < 0 || dev >= 64) {
+        *err = cuda_error(e, "cudaGetDevice");
+        return nullptr;
+    }
+    std::lock_guard<std::mutex> g(g_ctx_mu);
+    if (!g_ctx[dev]) {
+        std::unique_ptr<Context> c(new Context());
+        c->device = dev;
+        e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) {
+            *err = cuda_error(e, "cudaStreamCreate");
+            return nullptr;
+        }
+        g_ctx[dev] = c.release();
+    }
+    return g_ctx[dev];
+}
+
+// ===========================================================================
+// Threshold keys
+// ===========================================================================
+// The reference's test, evaluated in the series dtype exactly as its CPU code
+// does it: f(v) = sqrt(v) (Euclidean, v = squared sum) or v (maximal), then
+// (t - f(v)) >= 0.  `volatile` keeps each step a separately rounded float
+// operation on every host ABI.
+static bool key_pred_f32(float t, float v, int norm) {
+    volatile float d = norm == DST_EUCLIDEAN ? std::sqrt(v) : v;
+    volatile float diff = t - d;
+    return diff >= 0.0f;
+}
+
+static bool key_pred_f64(double t, double v, int norm) {
+    volatile double d = norm == DST_EUCLIDEAN ? std::sqrt(v) : v;
+    volatile double diff = t - d;
+    return diff >= 0.0;
+}
+
+uint64_t threshold_key_f32(float t, int norm) {
+    const float never = -1.0f;
+    uint32_t never_bits;
+    std::memcpy(&never_bits, &never, 4);
+    auto val = [](uint32_t b) {
+        float f;
+        std::memcpy(&f, &b, 4);
+        return f;
+    };
+    if (!key_pred_f32(t, 0.0f, norm)) return never_bits;
+    uint32_t lo = 0u, hi = 0x7F7FFFFFu;   // +0 .. FLT_MAX, ordered by bit pattern
+    if (key_pred_f32(t, val(hi), norm)) return hi;
+    while (hi - lo > 1u) {                // pred(lo) holds, pred(hi) does not
+        uint32_t mid = lo + (hi - lo) / 2u;
+        if (key_pred_f32(t, val(mid), norm)) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+uint64_t threshold_key_f64(double t, int norm) {
+    auto val = [](uint64_t b) {
+        double f;
+        std::memcpy(&f, &b, 8);
+        return f;
+    };
+    if (!key_pred_f64(t, 0.0, norm)) return 0ull;
+    uint64_t lo = 0ull, hi = 0x7FEFFFFFFFFFFFFFull;   // +0 .. DBL_MAX
+    if (key_pred_f64(t, val(hi), norm)) return hi + 1ull;
+    while (hi - lo > 1ull) {
+        uint64_t mid = lo + (hi - lo) / 2ull;
+        if (key_pred_f64(t, val(mid), norm)) lo = mid;
+        else hi = mid;
+    }
+    return lo + 1ull;
+}
+
+static const uint64_t kNeverF32 = 0xBF800000ull;   // bits of -1.0f
+static const uint64_t kNeverF64 = 0ull;
+
+// ===========================================================================
+// Pass planning
+// ===========================================================================
+template <typename T>
+static void fill_desc(accrqa_walk_desc &d, int kind, const T *d_x, int64_t n,
+                      int tau, int emb, const T *thr, int k0, int cnt, int norm) {
+    std::memset(&d, 0, sizeof(d));
+    d.kind = kind;
+    d.dtype = DType<T>::code;
+    d.norm = norm;
+    d.tau = tau;
+    d.emb = emb;
+    d.nthr = cnt;
+    d.nc = n - (int64_t)(emb - 1) * tau;
+    d.d_x = d_x;
+    const uint64_t never = DType<T>::code == ACCRQA_F32 ? kNeverF32 : kNeverF64;
+    for (int k = 0; k < ACCRQA_MAX_THR_PER_PASS; k++)
+        d.keys[k] = k < cnt ? threshold_key<T>(thr[k0 + k], norm) : never;
+}
+
+template <typename T>
+Accrqa_Error enqueue_rr(const T *d_x, int64_t n, int tau, int emb, const T *thr,
+                        int nthr, int norm, uint64_t *d_counts, cudaStream_t st) {
+    for (int k0 = 0; k0 < nthr; k0 += ACCRQA_MAX_THR_PER_PASS) {
+        int cnt = nthr - k0 < ACCRQA_MAX_THR_PER_PASS ? nthr - k0 : ACCRQA_MAX_THR_PER_PASS;
+        accrqa_walk_desc d;
+        fill_desc<T>(d, ACCRQA_WALK_RR, d_x, n, tau, emb, thr, k0, cnt, norm);
+        d.d_counts = d_counts + k0;
+        int e = accrqa_gb300_launch_walk(&d, st);
+        if (e) return cuda_error((cudaError_t)e, "RR kernel launch");
+    }
+    return SUCCESS;
+}
+
+template <typename T>
+Accrqa_Error enqueue_lines(int kind, const T *d_x, int64_t n, int tau, int emb,
+                           const T *thr, int nthr, int norm, uint64_t *d_hist,
+                           int64_t stride, uint32_t *d_maxlen, cudaStream_t st) {
+    for (int k0 = 0; k0 < nthr; k0 += ACCRQA_MAX_THR_PER_PASS) {
+        int cnt = nthr - k0 < ACCRQA_MAX_THR_PER_PASS ? nthr - k0 : ACCRQA_MAX_THR_PER_PASS;
+        accrqa_walk_desc d;
+        fill_desc<T>(d, kind, d_x, n, tau, emb, thr, k0, cnt, norm);
+        d.d_hist = d_hist + (int64_t)k0 * stride;
+        d.hist_stride = stride;
+        d.d_maxlen = d_maxlen + k0;
+        int e = accrqa_gb300_launch_walk(&d, st);
+        if (e) return cuda_error((cudaError_t)e, kind == ACCRQA_WALK_DET ? "DET kernel launch" : "LAM kernel launch");
+    }
+    return SUCCESS;
+}
+
+template Accrqa_Error enqueue_rr<float>(const float *, int64_t, int, int, const float *, int, int, uint64_t *, cudaStream_t);
+template Accrqa_Error enqueue_rr<double>(const double *, int64_t, int, int, const double *, int, int, uint64_t *, cudaStream_t);
+template Accrqa_Error enqueue_lines<float>(int, const float *, int64_t, int, int, const float *, int, int, uint64_t *, int64_t, uint32_t *, cudaStream_t);
+template Accrqa_Error enqueue_lines<double>(int, const double *, int64_t, int, int, const double *, int, int, uint64_t *, int64_t, uint32_t *, cudaStream_t);
+
+// ===========================================================================
+// Histogram post-processing
+// ===========================================================================
+LineHistogram::LineHistogram(std::vector<uint64_t> prefix, uint64_t h_last,
+                             int64_t nc)
+    : h_(std::move(prefix)), h_last_(h_last), nc_(nc) {
+    p_ = (int64_t)h_.size();
+    if (p_ > nc_ + 1) {
+        h_.resize((size_t)(nc_ + 1));
+        p_ = nc_ + 1;
+    }
+    if (p_ == nc_ + 1) h_last_ = h_[(size_t)nc_];
+    m_.resize((size_t)p_);
+    s_.resize((size_t)p_);
+    uint64_t m = 0, s = 0;
+    if (p_ <= nc_) {
+        m = (uint64_t)nc_ * h_last_;
+        s = h_last_;
+    }
+    for (int64_t l = p_ - 1; l >= 0; l--) {
+        m += (uint64_t)l * h_[(size_t)l];
+        s += h_[(size_t)l];
+        m_[(size_t)l] = m;
+        s_[(size_t)l] = s;
+    }
+}
+
+uint64_t LineHistogram::bin(int64_t l) const {
+    if (l >= 0 && l < p_) return h_[(size_t)l];
+    if (l == nc_) return h_last_;
+    return 0;
+}
+
+uint64_t LineHistogram::metric(int64_t l) const {
+    if (l < 0 || l > nc_) return 0;
+    if (l < p_) return m_[(size_t)l];
+    return (uint64_t)nc_ * h_last_;
+}
+
+uint64_t LineHistogram::scan(int64_t l) const {
+    if (l < 0 || l > nc_) return 0;
+    if (l < p_) return s_[(size_t)l];
+    return h_last_;
+}
+
+// src/AccRQA_functions.cpp:48-58
+double LineHistogram::primary(int64_t lmin) const {
+    uint64_t m0 = metric(0);
+    if (m0 > 0) return (double)metric(lmin) / (double)m0;
+    return NAN;
+}
+
+// src/AccRQA_functions.cpp:60-66
+double LineHistogram::secondary(int64_t lmin) const {
+    uint64_t s = scan(lmin);
+    if (s > 0) return (double)metric(lmin) / (double)s;
+    return NAN;
+}
+
+// Longest line: the reference's binary search over scan[], step for step
+// (src/AccRQA_functions.cpp:68-112), so that its corner cases carry over.
+double LineHistogram::tertiary(int is_det) const {
+    const uint64_t hs = (uint64_t)nc_ + 1;
+    uint64_t end = hs - 1, mid = hs / 2, start = 0, length = hs;
+    const uint64_t last = is_det == 1 ? scan((int64_t)end) : 0;
+    for (;;) {
+        const uint64_t mid_value = scan((int64_t)mid);
+        const uint64_t midm1_value = mid > 0 ? scan((int64_t)mid - 1) : 0;
+        if (mid_value == last && midm1_value > mid_value) {
+            mid = mid - 1;
+            break;
+        } else if (length == 0) {
+            break;
+        } else if (mid == 0) {
+            break;
+        } else if (mid_value > last) {
+            start = mid;
+            length = end - start;
+            mid = mid + (length + 1) / 2;
+        } else if (mid_value == last && midm1_value == last) {
+            end = mid;
+            length = end - start;
+            mid = start + (length >> 1);
+        }
+    }
+    return (double)mid;
+}
+
+// Entropy over lengths >= lmin (src/AccRQA_functions.cpp:114-124).  Zero
+// bins add nothing (p > 0 fails, also for 0/0), so only the non-zero prefix
+// and the last bin are visited, in ascending order as in the reference.
+double LineHistogram::quaternary(int64_t lmin) const {
+    double entr = 0;
+    const double denom = (double)scan(lmin);
+    int64_t f = lmin < 0 ? 0 : lmin;
+    for (; f < p_; f++) {
+        double p = (double)h_[(size_t)f] / denom;
+        if (p > 0) {
+            double t = p * std::log(p);
+            entr = entr + t;
+        }
+    }
+    if (p_ <= nc_ && lmin <= nc_) {
+        double p = (double)h_last_ / denom;
+        if (p > 0) {
+            double t = p * std::log(p);
+            entr = entr + t;
+        }
+    }
+    return (-1.0) * entr;
+}
+
+// src/AccRQA_functions.cpp:126-133
+double LineHistogram::rr() const {
+    return (double)metric(0) / (double)(nc_ * nc_);
+}
+
+// ===========================================================================
+// Shared helpers for the drivers
+// ===========================================================================
+template <typename T>
+static Accrqa_Error upload_series(Context &c, const T *x, int64_t n, const T **d_x) {
+    const size_t bytes = (size_t)(n + ACCRQA_SERIES_PAD) * sizeof(T);
+    CU(c.series.reserve(bytes), "cudaMalloc(series)");
+    CU(cudaMemcpyAsync(c.series.ptr, x, (size_t)n * sizeof(T), cudaMemcpyHostToDevice,
+                       c.stream), "cudaMemcpy(series H2D)");
+    CU(cudaMemsetAsync((T *)c.series.ptr + n, 0, ACCRQA_SERIES_PAD * sizeof(T), c.stream),
+       "cudaMemset(series pad)");
+    *d_x = (const T *)c.series.ptr;
+    return SUCCESS;
+}
+
+static int64_t embedded_length(size_t n, int tau, int emb) {
+    return (int64_t)n - (int64_t)(emb - 1) * (int64_t)tau;
+}
+
+static Accrqa_Error check_combo(size_t n, int tau, int emb) {
+    if (tau < 1 || emb < 1) {
+        set_last_error("tau (%d) and emb (%d) must be >= 1", tau, emb);
+        return ERR_INVALID_ARGUMENT;
+    }
+    if (embedded_length(n, tau, emb) < 1) {
+        set_last_error("series of %zu samples is too short for tau=%d, emb=%d", n, tau, emb);
+        return ERR_INVALID_ARGUMENT;
+    }
+    if ((int64_t)n > (int64_t)1 << 31) {
+        set_last_error("series longer than 2^31 samples are not supported");
+        return ERR_INVALID_ARGUMENT;
+    }
+    return SUCCESS;
+}
+
+static Accrqa_Error check_norm(int norm) {
+    if (norm != DST_EUCLIDEAN && norm != DST_MAXIMAL) {
+        set_last_error("invalid distance type %d", norm);
+        return ERR_INVALID_ARGUMENT;
+    }
+    return SUCCESS;
+}
+
+// Bytes of device histogram memory one batch of line passes may use.
+static size_t line_budget_bytes() {
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+        cudaGetLastError();
+        return (size_t)1 << 30;
+    }
+    size_t b = free_b / 4;
+    const size_t cap = (size_t)8 << 30;
+    return b < cap ? b : cap;
+}
+
+// Copy back the non-zero prefix of nthr histograms and wrap them.
+static Accrqa_Error fetch_histograms(Context &c, int kind, const uint64_t *d_hist,
+                                     int64_t stride, const uint32_t *d_maxlen,
+                                     int nthr, int64_t nc,
+                                     std::vector<LineHistogram> &out) {
+    std::vector<uint32_t> maxlen((size_t)nthr);
+    CU(cudaMemcpyAsync(maxlen.data(), d_maxlen, (size_t)nthr * 4, cudaMemcpyDeviceToHost,
+                       c.stream), "cudaMemcpy(maxlen D2H)");
+    CU(cudaStreamSynchronize(c.stream), "line kernels");
+    uint32_t mx = 0;
+    for (uint32_t v : maxlen) mx = v > mx ? v : mx;
+    int64_t p = (int64_t)(mx + 1 > ACCRQA_SHORT_RUN_BINS ? mx + 1 : ACCRQA_SHORT_RUN_BINS);
+    if (p > nc + 1) p = nc + 1;
+    std::vector<uint64_t> buf((size_t)p * nthr);
+    CU(cudaMemcpy2DAsync(buf.data(), (size_t)p * 8, d_hist, (size_t)stride * 8,
+                         (size_t)p * 8, (size_t)nthr, cudaMemcpyDeviceToHost, c.stream),
+       "cudaMemcpy(histogram D2H)");
+    CU(cudaStreamSynchronize(c.stream), "histogram copy");
+    out.clear();
+    out.reserve((size_t)nthr);
+    for (int k = 0; k < nthr; k++) {
+        std::vector<uint64_t> h(buf.begin() + (size_t)k * p, buf.begin() + (size_t)(k + 1) * p);
+        uint64_t last = 0;
+        if (kind == ACCRQA_WALK_DET) {
+            // Upper-triangle runs doubled, plus the line of identity
+            // (src/AccRQA_CPU_function.cpp:156-162).
+            for (auto &v : h) v = 2 * v;
+            if (p == nc + 1) h[(size_t)nc] += 1;
+            else last = 1;
+        }
+        out.emplace_back(std::move(h), last, nc);
+    }
+    return SUCCESS;
+}
+
+// ===========================================================================
+// API-level drivers
+// ===========================================================================
+template <typename T>
+Accrqa_Error run_rr(T *out, const T *x, size_t n, const int *taus, int ntau,
+                    const int *embs, int nemb, const T *thr, int nthr, int norm) {
+    Accrqa_Error err = check_norm(norm);
+    if (err) return err;
+    for (int a = 0; a < ntau; a++)
+        for (int b = 0; b < nemb; b++)
+            if ((err = check_combo(n, taus[a], embs[b]))) return err;
+    err = SUCCESS;
+    Context *c = current_context(&err);
+    if (!c) return err;
+    std::lock_guard<std::mutex> g(c->mu);
+    const T *d_x = nullptr;
+    if ((err = upload_series<T>(*c, x, (int64_t)n, &d_x))) return err;
+    const size_t ncnt = (size_t)ntau * nemb * nthr;
+    CU(c->counts.reserve(ncnt * 8), "cudaMalloc(counts)");
+    uint64_t *d_counts = (uint64_t *)c->counts.ptr;
+    CU(cudaMemsetAsync(d_counts, 0, ncnt * 8, c->stream), "cudaMemset(counts)");
+    for (int a = 0; a < ntau; a++)
+        for (int b = 0; b < nemb; b++) {
+            uint64_t *dst = d_counts + ((size_t)a * nemb + b) * nthr;
+            if ((err = enqueue_rr<T>(d_x, (int64_t)n, taus[a], embs[b], thr, nthr, norm,
+                                     dst, c->stream)))
+                return err;
+        }
+    std::vector<uint64_t> counts(ncnt);
+    CU(cudaMemcpyAsync(counts.data(), d_counts, ncnt * 8, cudaMemcpyDeviceToHost, c->stream),
+       "cudaMemcpy(counts D2H)");
+    CU(cudaStreamSynchronize(c->stream), "RR kernels");
+    for (int a = 0; a < ntau; a++)
+        for (int b = 0; b < nemb; b++) {
+            const int64_t nc = embedded_length(n, taus[a], embs[b]);
+            for (int k = 0; k < nthr; k++) {
+                const size_t pos = ((size_t)a * nemb + b) * nthr + k;
+                // src/AccRQA_functions.cpp:884
+                out[pos] = (T)((double)counts[pos] / (double)(nc * nc));
+            }
+        }
+    return SUCCESS;
+}
+
+template <typename T>
+Accrqa_Error run_lines(int kind, T *out, const T *x, size_t n, const int *taus,
+                       int ntau, const int *embs, int nemb, const int *lmins,
+                       int nl, const T *thr, int nthr, int norm, int calc_entr) {
+    Accrqa_Error err = check_norm(norm);
+    if (err) return err;
+    int lmin_max = 0;
+    for (int l = 0; l < nl; l++) {
+        if (lmins[l] < 0) {
+            set_last_error("minimal line length %d must be >= 0", lmins[l]);
+            return ERR_INVALID_ARGUMENT;
+        }
+        if (lmins[l] > lmin_max) lmin_max = lmins[l];
+    }
+    for (int a = 0; a < ntau; a++)
+        for (int b = 0; b < nemb; b++)
+            if ((err = check_combo(n, taus[a], embs[b]))) return err;
+    // src/AccRQA_functions.cpp:499-506 / :754-761
+    const bool full = calc_entr == 1 || lmin_max >= 16;
+    const bool is_det = kind == ACCRQA_WALK_DET;
+
+    err = SUCCESS;
+    Context *c = current_context(&err);
+    if (!c) return err;
+    std::lock_guard<std::mutex> g(c->mu);
+    const T *d_x = nullptr;
+    if ((err = upload_series<T>(*c, x, (int64_t)n, &d_x))) return err;
+
+    const size_t budget = line_budget_bytes();
+    int combo = 0;
+    const int ncombo = ntau * nemb;
+    while (combo < ncombo) {
+        // one batch: consecutive (tau, emb) combos whose histograms fit the budget
+        int first = combo;
+        size_t used = 0;
+        std::vector<int64_t> off;
+        while (combo < ncombo) {
+            const int64_t nc = embedded_length(n, taus[combo / nemb], embs[combo % nemb]);
+            const size_t need = (size_t)nthr * (size_t)(nc + 1) * 8;
+            if (combo > first && used + need > budget) break;
+            off.push_back((int64_t)(used / 8));
+            used += need;
+            combo++;
+        }
+        const int last = combo;
+        CU(c->hist.reserve(used), "cudaMalloc(histograms)");
+        CU(c->maxlen.reserve((size_t)(last - first) * nthr * 4), "cudaMalloc(maxlen)");
+        uint64_t *d_hist = (uint64_t *)c->hist.ptr;
+        uint32_t *d_max = (uint32_t *)c->maxlen.ptr;
+        CU(cudaMemsetAsync(d_hist, 0, used, c->stream), "cudaMemset(histograms)");
+        CU(cudaMemsetAsync(d_max, 0, (size_t)(last - first) * nthr * 4, c->stream),
+           "cudaMemset(maxlen)");
+        for (int q = first; q < last; q++) {
+            const int tau = taus[q / nemb], emb = embs[q % nemb];
+            const int64_t nc = embedded_length(n, tau, emb);
+            if ((err = enqueue_lines<T>(kind, d_x, (int64_t)n, tau, emb, thr, nthr, norm,
+                                        d_hist + off[(size_t)(q - first)], nc + 1,
+                                        d_max + (size_t)(q - first) * nthr, c->stream)))
+                return err;
+        }
+        for (int q = first; q < last; q++) {
+            const int a = q / nemb, b = q % nemb;
+            const int64_t nc = embedded_length(n, taus[a], embs[b]);
+            std::vector<LineHistogram> hs;
+            if ((err = fetch_histograms(*c, kind, d_hist + off[(size_t)(q - first)], nc + 1,
+                                        d_max + (size_t)(q - first) * nthr, nthr, nc, hs)))
+                return err;
+            for (int k = 0; k < nthr; k++) {
+                const LineHistogram &h = hs[(size_t)k];
+                const double lmax = full ? h.tertiary(is_det ? 1 : 0) : NAN;
+                double rr;
+                if (full) {
+                    rr = h.rr();
+                } else {
+                    // (nc-1)^2 in unsigned arithmetic, as the boxcar wrappers
+                    // compute it (src/AccRQA-GPU-HST.cu:2249,2635)
+                    const uint64_t d1 = (uint64_t)nc - 1;
+                    rr = (double)h.metric(0) / (double)(d1 * d1);
+                }
+                for (int l = 0; l < nl; l++) {
+                    // src/AccRQA_functions.cpp:407-412 / :581-590
+                    const size_t pos = (size_t)a * nl * nemb * nthr + (size_t)b * nl * nthr +
+                                       (size_t)l * nthr + k;
+                    out[5 * pos + 0] = (T)h.primary(lmins[l]);
+                    out[5 * pos + 1] = (T)h.secondary(lmins[l]);
+                    out[5 * pos + 2] = (T)lmax;
+                    out[5 * pos + 3] = (T)(full ? h.quaternary(lmins[l]) : NAN);
+                    out[5 * pos + 4] = (T)rr;
+                }
+            }
+        }
+    }
+    return SUCCESS;
+}
+
+template <typename T, typename OUT>
+Accrqa_Error run_rp(OUT *out, const T *x, size_t n, int tau, int emb, T thr, int norm) {
+    Accrqa_Error err = check_norm(norm);
+    if (err) return err;
+    if ((err = check_combo(n, tau, emb))) return err;
+    err = SUCCESS;
+    Context *c = current_context(&err);
+    if (!c) return err;
+    std::lock_guard<std::mutex> g(c->mu);
+    const T *d_x = nullptr;
+    if ((err = upload_series<T>(*c, x, (int64_t)n, &d_x))) return err;
+    const int64_t nc = embedded_length(n, tau, emb);
+    const uint64_t key = threshold_key<T>(thr, norm);
+    const size_t row_bytes = (size_t)nc * sizeof(OUT);
+    size_t chunk_bytes = (size_t)256 << 20;
+    int64_t rows = (int64_t)(chunk_bytes / row_bytes);
+    if (rows < 1) rows = 1;
+    if (rows > nc) rows = nc;
+    CU(c->rp[0].reserve((size_t)rows * row_bytes), "cudaMalloc(RP chunk)");
+    for (int64_t r0 = 0; r0 < nc; r0 += rows) {
+        const int64_t nr = nc - r0 < rows ? nc - r0 : rows;
+        int e = accrqa_gb300_launch_rp(d_x, DType<T>::code, norm, nc, tau, emb, key,
+                                       c->rp[0].ptr, sizeof(OUT) == 1 ? 1 : 2, r0, nr,
+                                       c->stream);
+        if (e) return cuda_error((cudaError_t)e, "RP kernel launch");
+        CU(cudaMemcpyAsync(out + r0 * nc, c->rp[0].ptr, (size_t)nr * row_bytes,
+                           cudaMemcpyDeviceToHost, c->stream), "cudaMemcpy(RP D2H)");
+        CU(cudaStreamSynchronize(c->stream), "RP kernel");
+    }
+    return SUCCESS;
+}
+
+template <typename T>
+Accrqa_Error raw_rr_counts(uint64_t *counts, const T *x, int64_t n, int tau, int emb,
+                           const T *thr, int nthr, int norm) {
+    Accrqa_Error err = check_norm(norm);
+    if (err) return err;
+    if ((err = check_combo((size_t)n, tau, emb))) return err;
+    if (nthr < 1) {
+        set_last_error("nthr must be >= 1");
+        return ERR_INVALID_ARGUMENT;
+    }
+    err = SUCCESS;
+    Context *c = current_context(&err);
+    if (!c) return err;
+    std::lock_guard<std::mutex> g(c->mu);
+    const T *d_x = nullptr;
+    if ((err = upload_series<T>(*c, x, n, &d_x))) return err;
+    CU(c->counts.reserve((size_t)nthr * 8), "cudaMalloc(counts)");
+    CU(cudaMemsetAsync(c->counts.ptr, 0, (size_t)nthr * 8, c->stream), "cudaMemset(counts)");
+    if ((err = enqueue_rr<T>(d_x, n, tau, emb, thr, nthr, norm, (uint64_t *)c->counts.ptr,
+                             c->stream)))
+        return err;
+    CU(cudaMemcpyAsync(counts, c->counts.ptr, (size_t)nthr * 8, cudaMemcpyDeviceToHost,
+                       c->stream), "cudaMemcpy(counts D2H)");
+    CU(cudaStreamSynchronize(c->stream), "RR kernels");
+    return SUCCESS;
+}
+
+template <typename T>
+Accrqa_Error raw_histograms(int kind, uint64_t *hist, const T *x, int64_t n, int tau,
+                            int emb, const T *thr, int nthr, int norm) {
+    Accrqa_Error err = check_norm(norm);
+    if (err) return err;
+    if ((err = check_combo((size_t)n, tau, emb))) return err;
+    if (nthr < 1) {
+        set_last_error("nthr must be >= 1");
+        return ERR_INVALID_ARGUMENT;
+    }
+    err = SUCCESS;
+    Context *c = current_context(&err);
+    if (!c) return err;
+    std::lock_guard<std::mutex> g(c->mu);
+    const T *d_x = nullptr;
+    if ((err = upload_series<T>(*c, x, n, &d_x))) return err;
+    const int64_t nc = embedded_length((size_t)n, tau, emb);
+    const size_t bytes = (size_t)nthr * (size_t)(nc + 1) * 8;
+    CU(c->hist.reserve(bytes), "cudaMalloc(histograms)");
+    CU(c->maxlen.reserve((size_t)nthr * 4), "cudaMalloc(maxlen)");
+    CU(cudaMemsetAsync(c->hist.ptr, 0, bytes, c->stream), "cudaMemset(histograms)");
+    CU(cudaMemsetAsync(c->maxlen.ptr, 0, (size_t)nthr * 4, c->stream), "cudaMemset(maxlen)");
+    if ((err = enqueue_lines<T>(kind, d_x, n, tau, emb, thr, nthr, norm,
+                                (uint64_t *)c->hist.ptr, nc + 1, (uint32_t *)c->maxlen.ptr,
+                                c->stream)))
+        return err;
+    CU(cudaMemcpyAsync(hist, c->hist.ptr, bytes, cudaMemcpyDeviceToHost, c->stream),
+       "cudaMemcpy(histograms D2H)");
+    CU(cudaStreamSynchronize(c->stream), "line kernels");
+    if (kind == ACCRQA_WALK_DET) {
+        for (int k = 0; k < nthr; k++) {
+            uint64_t *h = hist + (size_t)k * (nc + 1);
+            for (int64_t l = 0; l <= nc; l++) h[l] = 2 * h[l];
+            h[nc] += 1;
+        }
+    }
+    return SUCCESS;
+}
+
+// explicit instantiations
+template Accrqa_Error run_rr<float>(float *, const float *, size_t, const int *, int, const int *, int, const float *, int, int);
+template Accrqa_Error run_rr<double>(double *, const double *, size_t, const int *, int, const int *, int, const double *, int, int);
+template Accrqa_Error run_lines<float>(int, float *, const float *, size_t, const int *, int, const int *, int, const int *, int, const float *, int, int, int);
+template Accrqa_Error run_lines<double>(int, double *, const double *, size_t, const int *, int, const int *, int, const int *, int, const double *, int, int, int);
+template Accrqa_Error run_rp<float, char>(char *, const float *, size_t, int, int, float, int);
+template Accrqa_Error run_rp<float, int>(int *, const float *, size_t, int, int, float, int);
+template Accrqa_Error run_rp<double, char>(char *, const double *, size_t, int, int, double, int);
+template Accrqa_Error run_rp<double, int>(int *, const double *, size_t, int, int, double, int);
+template Accrqa_Error raw_rr_counts<float>(uint64_t *, const float *, int64_t, int, int, const float *, int, int);
+template Accrqa_Error raw_rr_counts<double>(uint64_t *, const double *, int64_t, int, int, const double *, int, int);
+template Accrqa_Error raw_histograms<float>(int, uint64_t *, const float *, int64_t, int, int, const float *, int, int);
+template Accrqa_Error raw_histograms<double>(int, uint64_t *, const double *, int64_t, int, int, const double *, int, int);
+
+}  // namespace accrqa

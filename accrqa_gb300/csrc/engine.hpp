@@ -1,0 +1,120 @@
+// engine.hpp -- host side of the GB300 RQA engine: device context, threshold
+// keys, pass planning over (tau, emb, threshold) and histogram
+// post-processing.  Compiled with the host C++ compiler; talks to the
+// kernels only through engine_abi.h.
+#ifndef ACCRQA_GB300_ENGINE_HPP
+#define ACCRQA_GB300_ENGINE_HPP
+
+#include <cuda_runtime_api.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <mutex>
+#include <vector>
+
+#include "../../include/accrqa_gb300.h"
+#include "engine_abi.h"
+
+namespace accrqa {
+
+typedef unsigned long long u64;
+
+// ---- errors ---------------------------------------------------------------
+void set_last_error(const char *fmt, ...);
+const char *last_error();
+Accrqa_Error cuda_error(cudaError_t e, const char *what);
+
+// ---- device memory --------------------------------------------------------
+// Grow-only device allocation owned by a context.
+struct DeviceBuffer {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+    cudaError_t reserve(size_t need);
+    void release();
+};
+
+// One per CUDA device: a stream, reusable buffers and a lock serialising the
+// calls that use them.
+struct Context {
+    int device = -1;
+    cudaStream_t stream = nullptr;
+    std::mutex mu;
+    DeviceBuffer series, counts, hist, maxlen, rp[2];
+    std::vector<uint64_t> host_u64;
+};
+
+// Context of the calling thread's current device, created on first use.
+// Returns nullptr and sets *err when no usable device exists.
+Context *current_context(Accrqa_Error *err);
+
+// ---- threshold keys -------------------------------------------------------
+uint64_t threshold_key_f32(float t, int norm);
+uint64_t threshold_key_f64(double t, int norm);
+template <typename T> inline uint64_t threshold_key(T t, int norm);
+template <> inline uint64_t threshold_key<float>(float t, int norm) { return threshold_key_f32(t, norm); }
+template <> inline uint64_t threshold_key<double>(double t, int norm) { return threshold_key_f64(t, norm); }
+
+template <typename T> struct DType;
+template <> struct DType<float> { static const int32_t code = ACCRQA_F32; };
+template <> struct DType<double> { static const int32_t code = ACCRQA_F64; };
+
+// ---- passes ----------------------------------------------------------------
+// Enqueue the passes for one (series, tau, emb) and nthr thresholds on st.
+// d_counts / d_hist / d_maxlen must be zeroed by the caller.
+template <typename T>
+Accrqa_Error enqueue_rr(const T *d_x, int64_t n, int tau, int emb, const T *thr,
+                        int nthr, int norm, uint64_t *d_counts, cudaStream_t st);
+template <typename T>
+Accrqa_Error enqueue_lines(int kind, const T *d_x, int64_t n, int tau, int emb,
+                           const T *thr, int nthr, int norm, uint64_t *d_hist,
+                           int64_t stride, uint32_t *d_maxlen, cudaStream_t st);
+
+// ---- post-processing --------------------------------------------------------
+// A length histogram H[0..nc] held as a dense prefix H[0..P) plus the single
+// bin H[nc] (all bins between are zero).  The accessors return the
+// reference's metric[] and scan[] arrays (src/AccRQA_CPU_function.cpp:181-204)
+// with wrapping 64-bit arithmetic; indices past nc read 0.
+class LineHistogram {
+  public:
+    LineHistogram(std::vector<uint64_t> prefix, uint64_t h_last, int64_t nc);
+    int64_t nc() const { return nc_; }
+    uint64_t bin(int64_t l) const;
+    uint64_t metric(int64_t l) const;
+    uint64_t scan(int64_t l) const;
+    // The five measures of src/AccRQA_functions.cpp:48-133.
+    double primary(int64_t lmin) const;
+    double secondary(int64_t lmin) const;
+    double tertiary(int is_det) const;
+    double quaternary(int64_t lmin) const;
+    double rr() const;
+
+  private:
+    std::vector<uint64_t> h_, m_, s_;   // prefix bins, suffix sums over the prefix
+    uint64_t h_last_ = 0;
+    int64_t nc_ = 0;
+    int64_t p_ = 0;                     // prefix length, <= nc + 1
+};
+
+// ---- API-level drivers (reference semantics) -------------------------------
+template <typename T>
+Accrqa_Error run_rr(T *out, const T *x, size_t n, const int *taus, int ntau,
+                    const int *embs, int nemb, const T *thr, int nthr, int norm);
+template <typename T>
+Accrqa_Error run_lines(int kind, T *out, const T *x, size_t n, const int *taus,
+                       int ntau, const int *embs, int nemb, const int *lmins,
+                       int nl, const T *thr, int nthr, int norm, int calc_entr);
+template <typename T, typename OUT>
+Accrqa_Error run_rp(OUT *out, const T *x, size_t n, int tau, int emb, T thr,
+                    int norm);
+
+// Raw results for the engine C ABI (full-convention histograms).
+template <typename T>
+Accrqa_Error raw_rr_counts(uint64_t *counts, const T *x, int64_t n, int tau,
+                           int emb, const T *thr, int nthr, int norm);
+template <typename T>
+Accrqa_Error raw_histograms(int kind, uint64_t *hist, const T *x, int64_t n,
+                            int tau, int emb, const T *thr, int nthr, int norm);
+
+}  // namespace accrqa
+
+#endif

@@ -1,0 +1,61 @@
+/* engine_abi.h -- the thin C ABI between the C++ host engine and the CUDA
+ * launch code.  Plain structs and pointers only; both sides are compiled
+ * separately (g++ for the host engine, nvcc for the kernels).
+ */
+#ifndef ACCRQA_GB300_ENGINE_ABI_H
+#define ACCRQA_GB300_ENGINE_ABI_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum accrqa_walk_kind {
+    ACCRQA_WALK_RR = 0,   /* recurrent-cell counts, full matrix */
+    ACCRQA_WALK_DET = 1,  /* raw strict-upper-triangle diagonal-run histograms */
+    ACCRQA_WALK_LAM = 2   /* row-run histograms of the full matrix */
+};
+
+enum accrqa_dtype { ACCRQA_F32 = 0, ACCRQA_F64 = 1 };
+
+#define ACCRQA_MAX_THR_PER_PASS 16
+#define ACCRQA_SERIES_PAD 128
+#define ACCRQA_SHORT_RUN_BINS 512
+
+/* One kernel pass: one (series, tau, emb, norm) and up to 16 thresholds. */
+typedef struct accrqa_walk_desc {
+    int32_t kind;            /* accrqa_walk_kind */
+    int32_t dtype;           /* accrqa_dtype */
+    int32_t norm;            /* 1 Euclidean, 2 maximal */
+    int32_t tau;
+    int32_t emb;
+    int32_t nthr;            /* 1..16 */
+    int64_t nc;              /* embedded length */
+    const void *d_x;         /* device series, >= n + ACCRQA_SERIES_PAD elements */
+    uint64_t keys[ACCRQA_MAX_THR_PER_PASS]; /* comparison keys (accrqa_gb300_threshold_keys) */
+    uint64_t *d_counts;      /* RR: [nthr] accumulated with atomics (zero first) */
+    uint64_t *d_hist;        /* DET/LAM: [nthr][hist_stride] (zero first) */
+    int64_t hist_stride;     /* >= nc + 1 */
+    uint32_t *d_maxlen;      /* DET/LAM: [nthr] longest line >= ACCRQA_SHORT_RUN_BINS */
+} accrqa_walk_desc;
+
+/* Enqueue one pass on `stream` (a cudaStream_t, 0 = legacy default stream).
+ * Returns 0 or a cudaError_t value. */
+int accrqa_gb300_launch_walk(const accrqa_walk_desc *desc, void *stream);
+
+/* Enqueue the recurrence plot of rows [row0, row0 + nrows) into d_out
+ * (row-major, nc columns; out_type 1 = int8, 2 = int32). */
+int accrqa_gb300_launch_rp(const void *d_x, int32_t dtype, int32_t norm,
+                           int64_t nc, int32_t tau, int32_t emb, uint64_t key,
+                           void *d_out, int32_t out_type, int64_t row0,
+                           int64_t nrows, void *stream);
+
+/* Number of streaming multiprocessors of the current device (cached). */
+int accrqa_gb300_sm_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

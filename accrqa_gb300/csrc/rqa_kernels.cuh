@@ -1,0 +1,365 @@
+// rqa_kernels.cuh -- the hot kernels of the GB300 RQA engine.
+//
+//   rr_rows   : recurrent-cell counts per threshold (RR), upper triangle by
+//               rows, one warp per 32-row band; replaces
+//               GPU_RQA_RR_seedsSM_improved_reduction_kernel
+//               (src/AccRQA-GPU-RR.cu:61-121).
+//   det_diags : diagonal-line histograms per threshold (DET), one lane per
+//               diagonal of the strict upper triangle, 32 diagonals per warp;
+//               replaces GPU_RQA_HST_length_histogram_diagonal and its scan /
+//               compaction helpers (src/AccRQA-GPU-HST.cu:34-74,209-240,440-480).
+//   lam_rows  : vertical-line histograms per threshold (LAM), one lane per
+//               row of the full matrix (the matrix is symmetric, rows and
+//               columns give the same histogram); replaces
+//               GPU_RQA_HST_length_histogram_vertical (src/AccRQA-GPU-HST.cu:401-438).
+//   rp_cells  : the recurrence plot itself (the reference computes it on the
+//               CPU only, src/AccRQA_CPU_function.cpp:226-244).
+//
+// All thresholds of a pass (up to 16) are decided from one distance
+// evaluation.  Lines are tracked as 32-bit masks per lane and threshold;
+// runs crossing mask boundaries are carried in registers along the line, so
+// no second pass or inter-block exchange is needed.  Work units pair band b
+// with band nbands-1-b so that every warp walks the same number of cells;
+// grids are persistent and warps stride over units.
+//
+// Memory contract: the series buffer holds at least n + kSeriesPad elements.
+// Blocks are evaluated 32 cells at a time without per-cell bounds on the
+// loads; cells past the end of a line read the pad and are masked out.
+#pragma once
+
+#include "rqa_device.cuh"
+
+namespace accrqa {
+
+constexpr int kWarpsPerCta = 4;
+constexpr int kSeriesPad = 128;
+
+// Distance between the register vector a[m] = x[i + m*tau] and the vector
+// starting at xj.  EMB = 0 is the generic instantiation (runtime emb, both
+// operands read from memory through xi).
+template <typename T, int NORM, int EMB>
+__device__ __forceinline__ T cell_dist(const T (&a)[EMB > 0 ? EMB : 1],
+                                       const T *__restrict__ xi,
+                                       const T *__restrict__ xj, long long tau,
+                                       int emb) {
+    T acc = T(0);
+    if (EMB > 0) {
+#pragma unroll
+        for (int m = 0; m < (EMB > 0 ? EMB : 1); m++)
+            acc = dist_step<T, NORM>(acc, a[m], __ldg(xj + m * tau), m == 0);
+    } else {
+        for (int m = 0; m < emb; m++)
+            acc = dist_step<T, NORM>(acc, __ldg(xi + m * tau), __ldg(xj + m * tau),
+                                     m == 0);
+    }
+    return acc;
+}
+
+// Distance with both operands read from memory.
+template <typename T, int NORM, int EMB>
+__device__ __forceinline__ T cell_dist_mem(const T *__restrict__ xi,
+                                           const T *__restrict__ xj,
+                                           long long tau, int emb) {
+    T acc = T(0);
+    if (EMB > 0) {
+#pragma unroll
+        for (int m = 0; m < (EMB > 0 ? EMB : 1); m++)
+            acc = dist_step<T, NORM>(acc, __ldg(xi + m * tau), __ldg(xj + m * tau),
+                                     m == 0);
+    } else {
+        for (int m = 0; m < emb; m++)
+            acc = dist_step<T, NORM>(acc, __ldg(xi + m * tau), __ldg(xj + m * tau),
+                                     m == 0);
+    }
+    return acc;
+}
+
+template <typename T, int EMB>
+__device__ __forceinline__ void load_lane_vec(T (&a)[EMB > 0 ? EMB : 1],
+                                              const T *__restrict__ xi,
+                                              long long tau) {
+    if (EMB > 0) {
+#pragma unroll
+        for (int m = 0; m < (EMB > 0 ? EMB : 1); m++) a[m] = __ldg(xi + m * tau);
+    }
+}
+
+// Shared-memory histogram set-up and flush, shared by the line kernels.
+__device__ __forceinline__ void hist_smem_clear(u32 *sh, u32 *shmax, int nbins) {
+    for (int t = threadIdx.x; t < nbins; t += blockDim.x) sh[t] = 0;
+    for (int t = threadIdx.x; t < kMaxThrPerPass; t += blockDim.x) shmax[t] = 0;
+    __syncthreads();
+}
+
+__device__ __forceinline__ void hist_smem_flush(const u32 *sh, const u32 *shmax,
+                                                const WalkArgs &p) {
+    __syncthreads();
+    for (int t = threadIdx.x; t < p.nthr * kShortRunBins; t += blockDim.x) {
+        u32 c = sh[t];
+        if (c) {
+            int k = t / kShortRunBins, l = t - k * kShortRunBins;
+            atomicAdd(&p.hist[(long long)k * p.hist_stride + l], (u64)c);
+        }
+    }
+    for (int t = threadIdx.x; t < p.nthr; t += blockDim.x)
+        if (shmax[t]) atomicMax(&p.maxlen[t], shmax[t]);
+}
+
+// ---------------------------------------------------------------------------
+// RR: lane r of a warp owns row i = 32*band + r and walks the columns j >= i;
+// the main-diagonal cell (i, i) is counted once, the others twice.
+// ---------------------------------------------------------------------------
+template <typename T, int NORM, int EMB, int NT>
+__global__ void __launch_bounds__(kWarpsPerCta * 32)
+rr_rows(const __grid_constant__ WalkArgs p) {
+    const T *__restrict__ x = (const T *)p.x;
+    const int lane = threadIdx.x & 31;
+    const long long gwarp = (long long)blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);
+    const long long nwarps = (long long)gridDim.x * kWarpsPerCta;
+    const long long nc = p.nc;
+    const long long tau = p.tau;
+
+    // Lane k keeps the 64-bit total of threshold k; per-band lane counters
+    // are 32-bit (a band walk adds at most nc per lane).
+    u64 total = 0;
+
+    for (long long unit = gwarp; unit < p.nunits; unit += nwarps) {
+#pragma unroll 1
+        for (int half = 0; half < 2; half++) {
+            const long long band = half == 0 ? unit : p.nbands - 1 - unit;
+            if (half == 1 && band == unit) break;
+            const long long i = band * 32 + lane;
+            const bool row_ok = i < nc;
+            T a[EMB > 0 ? EMB : 1];
+            load_lane_vec<T, EMB>(a, x + i, tau);
+            u32 up[NT], dg[NT];
+#pragma unroll
+            for (int k = 0; k < NT; k++) { up[k] = 0; dg[k] = 0; }
+            // first block: contains the main diagonal; checked cell by cell
+            {
+                const long long j0 = band * 32;
+#pragma unroll 4
+                for (int c = 0; c < 32; c++) {
+                    const long long j = j0 + c;
+                    T v = cell_dist<T, NORM, EMB>(a, x + i, x + j, tau, p.emb);
+                    const bool diag = row_ok && j == i;
+                    const bool upper = row_ok && j > i && j < nc;
+#pragma unroll
+                    for (int k = 0; k < NT; k++) {
+                        const bool r = is_rec(v, p.keys[k]);
+                        dg[k] += (diag && r) ? 1u : 0u;
+                        up[k] += (upper && r) ? 1u : 0u;
+                    }
+                }
+            }
+            // full blocks: j > i for every lane, all columns inside the matrix
+            long long j0 = band * 32 + 32;
+            for (; j0 + 32 <= nc; j0 += 32) {
+                const T *xj = x + j0;
+#pragma unroll 8
+                for (int c = 0; c < 32; c++) {
+                    T v = cell_dist<T, NORM, EMB>(a, x + i, xj + c, tau, p.emb);
+#pragma unroll
+                    for (int k = 0; k < NT; k++) up[k] += is_rec(v, p.keys[k]) ? 1u : 0u;
+                }
+            }
+            // tail block
+            if (j0 < nc) {
+#pragma unroll 4
+                for (int c = 0; c < 32; c++) {
+                    const long long j = j0 + c;
+                    T v = cell_dist<T, NORM, EMB>(a, x + i, x + j, tau, p.emb);
+                    const bool ok = row_ok && j < nc;
+#pragma unroll
+                    for (int k = 0; k < NT; k++) up[k] += (ok && is_rec(v, p.keys[k])) ? 1u : 0u;
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < NT; k++) {
+                u64 t = 2ull * (u64)(row_ok ? up[k] : 0u) + (u64)dg[k];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xFFFFFFFFu, t, o);
+                if (lane == k) total += t;
+            }
+        }
+    }
+    if (lane < p.nthr && lane < NT && total) atomicAdd(&p.counts[lane], total);
+}
+
+// ---------------------------------------------------------------------------
+// DET: lane q owns diagonal d = 1 + 32*band + q of the strict upper
+// triangle and walks its cells (s, s+d), s = 0 .. nc-d-1, 32 at a time.
+// The histogram written here is the raw upper-triangle histogram; doubling
+// and the line of identity are applied by the host.
+// ---------------------------------------------------------------------------
+template <typename T, int NORM, int EMB, int NT, bool CHECK>
+__device__ __forceinline__ void det_block(const T *__restrict__ xs,
+                                          const T *__restrict__ xsd,
+                                          long long tau, int emb, long long rem,
+                                          const WalkArgs &p, u32 (&carry)[NT],
+                                          const HistSink &sink) {
+    u32 mask[NT];
+#pragma unroll
+    for (int k = 0; k < NT; k++) mask[k] = 0;
+#pragma unroll 1
+    for (int g = 0; g < 32; g += 8) {
+        u32 m8[NT];
+#pragma unroll
+        for (int k = 0; k < NT; k++) m8[k] = 0;
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+            T v = cell_dist_mem<T, NORM, EMB>(xs + g + c, xsd + g + c, tau, emb);
+            const bool ok = !CHECK || (long long)(g + c) < rem;
+#pragma unroll
+            for (int k = 0; k < NT; k++)
+                m8[k] |= (ok && is_rec(v, p.keys[k])) ? (1u << c) : 0u;
+        }
+#pragma unroll
+        for (int k = 0; k < NT; k++) mask[k] |= m8[k] << g;
+    }
+#pragma unroll
+    for (int k = 0; k < NT; k++) runs_of_mask(mask[k], carry[k], k, sink);
+}
+
+template <typename T, int NORM, int EMB, int NT>
+__global__ void __launch_bounds__(kWarpsPerCta * 32)
+det_diags(const __grid_constant__ WalkArgs p) {
+    extern __shared__ u32 smem[];
+    u32 *sh = smem;
+    u32 *shmax = smem + NT * kShortRunBins;
+    hist_smem_clear(sh, shmax, NT * kShortRunBins);
+    const HistSink sink{sh, shmax, p.hist, p.hist_stride};
+
+    const T *__restrict__ x = (const T *)p.x;
+    const int lane = threadIdx.x & 31;
+    const long long gwarp = (long long)blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);
+    const long long nwarps = (long long)gridDim.x * kWarpsPerCta;
+    const long long nc = p.nc;
+    const long long tau = p.tau;
+
+    for (long long unit = gwarp; unit < p.nunits; unit += nwarps) {
+#pragma unroll 1
+        for (int half = 0; half < 2; half++) {
+            const long long band = half == 0 ? unit : p.nbands - 1 - unit;
+            if (half == 1 && band == unit) break;
+            const long long d = 1 + band * 32 + lane;
+            const long long len = nc - d;                 // cells on this diagonal
+            const long long wmin = nc - (band * 32 + 32); // shortest diagonal of the warp
+            const long long wmax = nc - (band * 32 + 1);  // longest diagonal of the warp
+            u32 carry[NT];
+#pragma unroll
+            for (int k = 0; k < NT; k++) carry[k] = 0;
+            long long s0 = 0;
+            for (; s0 + 32 <= wmin; s0 += 32)
+                det_block<T, NORM, EMB, NT, false>(x + s0, x + s0 + d, tau, p.emb,
+                                                   32, p, carry, sink);
+            for (; s0 < wmax; s0 += 32)
+                det_block<T, NORM, EMB, NT, true>(x + s0, x + s0 + d, tau, p.emb,
+                                                  len - s0, p, carry, sink);
+#pragma unroll
+            for (int k = 0; k < NT; k++)
+                if (carry[k]) sink.emit(k, carry[k]);
+        }
+    }
+    hist_smem_flush(sh, shmax, p);
+}
+
+// ---------------------------------------------------------------------------
+// LAM: lane r owns row i = 32*band + r of the full matrix and walks all
+// columns j = 0 .. nc-1, 32 at a time.  Every row has nc cells, so plain
+// band striding is balanced.
+// ---------------------------------------------------------------------------
+template <typename T, int NORM, int EMB, int NT, bool CHECK>
+__device__ __forceinline__ void lam_block(const T (&a)[EMB > 0 ? EMB : 1],
+                                          const T *__restrict__ xi,
+                                          const T *__restrict__ xj,
+                                          long long tau, int emb, long long rem,
+                                          const WalkArgs &p, u32 (&carry)[NT],
+                                          const HistSink &sink) {
+    u32 mask[NT];
+#pragma unroll
+    for (int k = 0; k < NT; k++) mask[k] = 0;
+#pragma unroll 1
+    for (int g = 0; g < 32; g += 8) {
+        u32 m8[NT];
+#pragma unroll
+        for (int k = 0; k < NT; k++) m8[k] = 0;
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+            T v = cell_dist<T, NORM, EMB>(a, xi, xj + g + c, tau, emb);
+            const bool ok = !CHECK || (long long)(g + c) < rem;
+#pragma unroll
+            for (int k = 0; k < NT; k++)
+                m8[k] |= (ok && is_rec(v, p.keys[k])) ? (1u << c) : 0u;
+        }
+#pragma unroll
+        for (int k = 0; k < NT; k++) mask[k] |= m8[k] << g;
+    }
+#pragma unroll
+    for (int k = 0; k < NT; k++) runs_of_mask(mask[k], carry[k], k, sink);
+}
+
+template <typename T, int NORM, int EMB, int NT>
+__global__ void __launch_bounds__(kWarpsPerCta * 32)
+lam_rows(const __grid_constant__ WalkArgs p) {
+    extern __shared__ u32 smem[];
+    u32 *sh = smem;
+    u32 *shmax = smem + NT * kShortRunBins;
+    hist_smem_clear(sh, shmax, NT * kShortRunBins);
+    const HistSink sink{sh, shmax, p.hist, p.hist_stride};
+
+    const T *__restrict__ x = (const T *)p.x;
+    const int lane = threadIdx.x & 31;
+    const long long gwarp = (long long)blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);
+    const long long nwarps = (long long)gridDim.x * kWarpsPerCta;
+    const long long nc = p.nc;
+    const long long tau = p.tau;
+
+    for (long long band = gwarp; band < p.nbands; band += nwarps) {
+        const long long i = band * 32 + lane;
+        const bool row_ok = i < nc;
+        T a[EMB > 0 ? EMB : 1];
+        load_lane_vec<T, EMB>(a, x + i, tau);
+        u32 carry[NT];
+#pragma unroll
+        for (int k = 0; k < NT; k++) carry[k] = 0;
+        long long j0 = 0;
+        if (row_ok) {
+            for (; j0 + 32 <= nc; j0 += 32)
+                lam_block<T, NORM, EMB, NT, false>(a, x + i, x + j0, tau, p.emb, 32, p,
+                                                   carry, sink);
+            if (j0 < nc)
+                lam_block<T, NORM, EMB, NT, true>(a, x + i, x + j0, tau, p.emb, nc - j0,
+                                                  p, carry, sink);
+#pragma unroll
+            for (int k = 0; k < NT; k++)
+                if (carry[k]) sink.emit(k, carry[k]);
+        }
+    }
+    hist_smem_flush(sh, shmax, p);
+}
+
+// ---------------------------------------------------------------------------
+// RP: one thread per 4 consecutive cells of a row, written as bytes or ints.
+// ---------------------------------------------------------------------------
+template <typename T, int NORM, typename OUT>
+__global__ void rp_cells(const T *__restrict__ x, long long nc, int tau, int emb,
+                         u64 key, OUT *__restrict__ out, long long row0,
+                         long long nrows) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long cpr = (nc + 3) / 4;             // 4-cell groups per row
+    const long long r = idx / cpr;
+    if (r >= nrows) return;
+    const long long j0 = (idx - r * cpr) * 4;
+    const long long i = row0 + r;
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        const long long j = j0 + c;
+        if (j < nc) {
+            T v = cell_dist_mem<T, NORM, 0>(x + i, x + j, tau, emb);
+            out[r * nc + j] = is_rec(v, key) ? OUT(1) : OUT(0);
+        }
+    }
+}
+
+}  // namespace accrqa

@@ -1,0 +1,103 @@
+// walk_dispatch.cuh -- picks the kernel instantiation for one pass and sizes
+// its persistent grid.  Included by the per-(kind, dtype) translation units
+// so that the instantiations compile in parallel.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "engine_abi.h"
+#include "rqa_kernels.cuh"
+
+namespace accrqa {
+
+int sm_count_cached();
+
+template <int KIND, typename T, int NORM, int EMB, int NT>
+static cudaError_t launch_one(const accrqa_walk_desc &d, cudaStream_t st) {
+    void (*kern)(WalkArgs);
+    size_t smem = 0;
+    if (KIND == ACCRQA_WALK_RR) {
+        kern = rr_rows<T, NORM, EMB, NT>;
+    } else if (KIND == ACCRQA_WALK_DET) {
+        kern = det_diags<T, NORM, EMB, NT>;
+        smem = (size_t)(NT * kShortRunBins + kMaxThrPerPass) * sizeof(u32);
+    } else {
+        kern = lam_rows<T, NORM, EMB, NT>;
+        smem = (size_t)(NT * kShortRunBins + kMaxThrPerPass) * sizeof(u32);
+    }
+    // Resident CTAs per SM for this instantiation, computed once.
+    static int per_sm = -1;
+    if (per_sm < 0) {
+        int v = 0;
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &v, kern, kWarpsPerCta * 32, smem);
+        if (e != cudaSuccess) return e;
+        per_sm = v > 0 ? v : 1;
+    }
+    WalkArgs a;
+    a.x = d.d_x;
+    a.nc = d.nc;
+    a.tau = d.tau;
+    a.emb = d.emb;
+    a.nthr = d.nthr;
+    a.pad_ = 0;
+    for (int k = 0; k < kMaxThrPerPass; k++) a.keys[k] = d.keys[k];
+    a.counts = (u64 *)d.d_counts;
+    a.hist = (u64 *)d.d_hist;
+    a.hist_stride = d.hist_stride;
+    a.maxlen = d.d_maxlen;
+    if (KIND == ACCRQA_WALK_LAM) {
+        a.nbands = (d.nc + 31) / 32;
+        a.nunits = a.nbands;
+    } else if (KIND == ACCRQA_WALK_RR) {
+        a.nbands = (d.nc + 31) / 32;
+        a.nunits = (a.nbands + 1) / 2;
+    } else {
+        a.nbands = (d.nc - 1 + 31) / 32;   // diagonals 1 .. nc-1
+        a.nunits = (a.nbands + 1) / 2;
+    }
+    if (a.nunits <= 0) return cudaSuccess;
+    long long want = (a.nunits + kWarpsPerCta - 1) / kWarpsPerCta;
+    long long cap = (long long)sm_count_cached() * per_sm;
+    int grid = (int)(want < cap ? want : cap);
+    kern<<<grid, kWarpsPerCta * 32, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <int KIND, typename T, int NORM, int EMB>
+static cudaError_t launch_nt(const accrqa_walk_desc &d, cudaStream_t st) {
+    if (d.nthr <= 4) return launch_one<KIND, T, NORM, EMB, 4>(d, st);
+    if (d.nthr <= 8) return launch_one<KIND, T, NORM, EMB, 8>(d, st);
+    return launch_one<KIND, T, NORM, EMB, 16>(d, st);
+}
+
+template <int KIND, typename T, int NORM>
+static cudaError_t launch_emb(const accrqa_walk_desc &d, cudaStream_t st) {
+    switch (d.emb) {
+        case 1: return launch_nt<KIND, T, NORM, 1>(d, st);
+        case 2: return launch_nt<KIND, T, NORM, 2>(d, st);
+        case 3: return launch_nt<KIND, T, NORM, 3>(d, st);
+        case 4: return launch_nt<KIND, T, NORM, 4>(d, st);
+        case 5: return launch_nt<KIND, T, NORM, 5>(d, st);
+        case 6: return launch_nt<KIND, T, NORM, 6>(d, st);
+        case 7: return launch_nt<KIND, T, NORM, 7>(d, st);
+        case 8: return launch_nt<KIND, T, NORM, 8>(d, st);
+        default: return launch_nt<KIND, T, NORM, 0>(d, st);
+    }
+}
+
+template <int KIND, typename T>
+static cudaError_t launch_walk_t(const accrqa_walk_desc &d, cudaStream_t st) {
+    if (d.norm == kNormEuclidean) return launch_emb<KIND, T, kNormEuclidean>(d, st);
+    if (d.norm == kNormMaximal) return launch_emb<KIND, T, kNormMaximal>(d, st);
+    return cudaErrorInvalidValue;
+}
+
+}  // namespace accrqa
+
+#define ACCRQA_DEFINE_WALK_TU(NAME, KIND, T)                                   \
+    namespace accrqa {                                                         \
+    cudaError_t NAME(const accrqa_walk_desc &d, cudaStream_t st) {             \
+        return launch_walk_t<KIND, T>(d, st);                                  \
+    }                                                                          \
+    }

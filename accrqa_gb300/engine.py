@@ -1,0 +1,158 @@
+"""Engine-level entry points of libaccrqa.so (numpy in, numpy out).
+
+These return the integers behind the RQA measures -- recurrent-cell counts
+and line-length histograms -- and are what the parity tests compare with the
+oracle.  The device-resident variants take raw device pointers (for example
+``tensor.data_ptr()``) and a CUDA stream handle.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+
+F32, F64 = 0, 1
+EUCLIDEAN, MAXIMAL = 1, 2
+NORMS = {"euclidean": EUCLIDEAN, "maximal": MAXIMAL, 1: EUCLIDEAN, 2: MAXIMAL}
+
+
+class EngineError(RuntimeError):
+    def __init__(self, code: int, what: str):
+        super().__init__(f"{what} failed with AccRQA error {code}: {_lib.last_error()}")
+        self.code = code
+
+
+def _check(code: int, what: str) -> None:
+    if code != 0:
+        raise EngineError(code, what)
+
+
+def _dtype_code(x: np.ndarray) -> int:
+    if x.dtype == np.float32:
+        return F32
+    if x.dtype == np.float64:
+        return F64
+    raise TypeError("series must be float32 or float64")
+
+
+def _norm(norm) -> int:
+    try:
+        return NORMS[norm]
+    except KeyError:
+        raise ValueError(f"unknown norm {norm!r}") from None
+
+
+def _vp(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _u64p(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))
+
+
+def embedded_length(n: int, tau: int, emb: int) -> int:
+    return n - (emb - 1) * tau
+
+
+def device_count() -> int:
+    return int(_lib.handle().accrqa_gb300_device_count())
+
+
+def threshold_keys(thresholds, dtype, norm) -> np.ndarray:
+    """Comparison keys the kernels use (see include/accrqa_gb300.h)."""
+    thr = np.ascontiguousarray(thresholds, dtype=dtype)
+    keys = np.zeros(len(thr), dtype=np.uint64)
+    _check(_lib.handle().accrqa_gb300_threshold_keys(
+        _u64p(keys), _vp(thr), _dtype_code(thr), len(thr), _norm(norm)),
+        "threshold_keys")
+    return keys
+
+
+def rr_counts(x, tau: int, emb: int, thresholds, norm) -> np.ndarray:
+    """Full-matrix recurrent-cell count per threshold (uint64)."""
+    x = np.ascontiguousarray(x)
+    thr = np.ascontiguousarray(thresholds, dtype=x.dtype)
+    out = np.zeros(len(thr), dtype=np.uint64)
+    _check(_lib.handle().accrqa_gb300_rr_counts(
+        _u64p(out), _vp(x), _dtype_code(x), len(x), tau, emb, _vp(thr), len(thr),
+        _norm(norm)), "rr_counts")
+    return out
+
+
+def _hist(fn_name, x, tau, emb, thresholds, norm):
+    x = np.ascontiguousarray(x)
+    thr = np.ascontiguousarray(thresholds, dtype=x.dtype)
+    nc = embedded_length(len(x), tau, emb)
+    out = np.zeros((len(thr), max(nc, 0) + 1), dtype=np.uint64)
+    _check(getattr(_lib.handle(), fn_name)(
+        _u64p(out), _vp(x), _dtype_code(x), len(x), tau, emb, _vp(thr), len(thr),
+        _norm(norm)), fn_name)
+    return out
+
+
+def det_histograms(x, tau: int, emb: int, thresholds, norm) -> np.ndarray:
+    """Diagonal-line histograms [nthr][nc+1] in the reference convention."""
+    return _hist("accrqa_gb300_det_histograms", x, tau, emb, thresholds, norm)
+
+
+def lam_histograms(x, tau: int, emb: int, thresholds, norm) -> np.ndarray:
+    """Vertical-line histograms [nthr][nc+1] over the full matrix."""
+    return _hist("accrqa_gb300_lam_histograms", x, tau, emb, thresholds, norm)
+
+
+def rp(x, tau: int, emb: int, threshold: float, norm, out_dtype=np.int8) -> np.ndarray:
+    """Recurrence plot [nc][nc] as int8 or int32."""
+    x = np.ascontiguousarray(x)
+    nc = embedded_length(len(x), tau, emb)
+    out = np.zeros((max(nc, 0), max(nc, 0)), dtype=out_dtype)
+    ot = 1 if np.dtype(out_dtype) == np.int8 else 2
+    _check(_lib.handle().accrqa_gb300_rp(
+        _vp(out), ot, _vp(x), _dtype_code(x), len(x), tau, emb, float(threshold),
+        _norm(norm)), "rp")
+    return out
+
+
+def measures(hist, lmin: int, is_det: bool) -> np.ndarray:
+    """{DET|LAM, L|TT, Lmax|TTmax, ENTR, RR} of one histogram (float64)."""
+    h = np.ascontiguousarray(hist, dtype=np.uint64)
+    out = np.zeros(5, dtype=np.float64)
+    _check(_lib.handle().accrqa_gb300_measures(
+        out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), _u64p(h), len(h), lmin,
+        1 if is_det else 0), "measures")
+    return out
+
+
+# ---------------------------------------------------------------------------
+# Device-resident passes (pointers into device memory, enqueue only)
+# ---------------------------------------------------------------------------
+def rr_counts_dev(d_counts: int, d_x: int, dtype_code: int, n: int, tau: int, emb: int,
+                  thresholds: np.ndarray, norm, stream: int = 0) -> None:
+    thr = np.ascontiguousarray(thresholds,
+                               dtype=np.float32 if dtype_code == F32 else np.float64)
+    _check(_lib.handle().accrqa_gb300_rr_counts_dev(
+        ctypes.c_void_p(d_counts), ctypes.c_void_p(d_x), dtype_code, n, tau, emb,
+        _vp(thr), len(thr), _norm(norm), ctypes.c_void_p(stream)), "rr_counts_dev")
+
+
+def _lines_dev(name, d_hist, stride, d_maxlen, d_x, dtype_code, n, tau, emb,
+               thresholds, norm, stream):
+    thr = np.ascontiguousarray(thresholds,
+                               dtype=np.float32 if dtype_code == F32 else np.float64)
+    _check(getattr(_lib.handle(), name)(
+        ctypes.c_void_p(d_hist), stride, ctypes.c_void_p(d_maxlen), ctypes.c_void_p(d_x),
+        dtype_code, n, tau, emb, _vp(thr), len(thr), _norm(norm),
+        ctypes.c_void_p(stream)), name)
+
+
+def det_hist_dev(d_hist, stride, d_maxlen, d_x, dtype_code, n, tau, emb, thresholds,
+                 norm, stream=0) -> None:
+    _lines_dev("accrqa_gb300_det_hist_dev", d_hist, stride, d_maxlen, d_x, dtype_code,
+               n, tau, emb, thresholds, norm, stream)
+
+
+def lam_hist_dev(d_hist, stride, d_maxlen, d_x, dtype_code, n, tau, emb, thresholds,
+                 norm, stream=0) -> None:
+    _lines_dev("accrqa_gb300_lam_hist_dev", d_hist, stride, d_maxlen, d_x, dtype_code,
+               n, tau, emb, thresholds, norm, stream)

@@ -1,0 +1,93 @@
+"""GPU parity: the engine's raw integers against the oracle, bit for bit.
+
+RR counts and DET/LAM line-length histograms from libaccrqa.so (through its
+C ABI) must equal the oracle restatement's exactly, for both dtypes, both
+norms, a spread of (tau, emb), thresholds that hit exact ties, and the edge
+cases the reference tests: constant input, tiny series, NaN/inf samples,
+negative and zero thresholds, more than 16 thresholds (several passes).
+"""
+import numpy as np
+import pytest
+
+from accrqa_gb300 import workloads
+
+pytestmark = pytest.mark.gpu
+
+NORMS = [1, 2]
+
+
+def _cases():
+    rng = np.random.default_rng(11)
+    cases = []
+    for dt in (np.float32, np.float64):
+        for norm in NORMS:
+            for (n, tau, emb) in [(97, 1, 1), (300, 1, 3), (451, 2, 5), (530, 3, 4),
+                                  (700, 1, 8), (256, 4, 2), (333, 7, 9), (129, 1, 2)]:
+                cases.append((dt, norm, n, tau, emb, int(rng.integers(0, 1 << 30))))
+    return cases
+
+
+@pytest.mark.parametrize("dt,norm,n,tau,emb,seed", _cases())
+def test_counts_and_histograms_match_oracle(gpu, oracle_mod, dt, norm, n, tau, emb, seed):
+    x = workloads.logistic(n, seed).astype(dt)
+    if seed % 3 == 0:
+        x = (np.round(x * 16) / 16).astype(dt)      # many exact ties at the thresholds
+    thr = np.array([0.0, 0.0625, 0.1, 0.125, 0.2, 0.25, 0.3, 0.5, 0.75, 1.0],
+                   dtype=dt)
+    rr = gpu.rr_counts(x, tau, emb, thr, norm)
+    np.testing.assert_array_equal(rr, oracle_mod.rr_counts(x, tau, emb, thr, norm))
+    det = gpu.det_histograms(x, tau, emb, thr, norm)
+    lam = gpu.lam_histograms(x, tau, emb, thr, norm)
+    for k, t in enumerate(thr):
+        np.testing.assert_array_equal(det[k], oracle_mod.det_hist(x, tau, emb, t, norm))
+        np.testing.assert_array_equal(lam[k], oracle_mod.lam_hist(x, tau, emb, t, norm))
+
+
+@pytest.mark.parametrize("nthr", [1, 3, 4, 5, 8, 9, 16, 17, 40])
+def test_threshold_pass_splitting(gpu, oracle_mod, nthr):
+    x = workloads.white(400, 5 + nthr).astype(np.float32)
+    thr = np.linspace(0.05, 3.0, nthr).astype(np.float32)
+    np.testing.assert_array_equal(gpu.rr_counts(x, 2, 3, thr, 1),
+                                  oracle_mod.rr_counts(x, 2, 3, thr, 1))
+    det = gpu.det_histograms(x, 2, 3, thr, 1)
+    for k, t in enumerate(thr):
+        np.testing.assert_array_equal(det[k], oracle_mod.det_hist(x, 2, 3, t, 1))
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_edge_series(gpu, oracle_mod, dt):
+    specials = {
+        "constant": np.ones(50),
+        "single": np.array([0.3]),
+        "two": np.array([0.1, 0.2]),
+        "nan_inf": np.array([0.1, np.nan, 0.3, np.inf, 0.2, -np.inf, 0.25, 0.26, 0.27,
+                             0.1, 0.3, 0.5] * 4),
+        "long_lines": np.tile(np.arange(10) / 10.0, 70),   # periodic: lines of length ~nc
+    }
+    thr = np.array([-1.0, -0.0, 0.0, 0.05, 0.1, 0.5, np.inf, np.nan], dtype=dt)
+    for name, s in specials.items():
+        x = s.astype(dt)
+        for norm in NORMS:
+            emb = 1 if len(x) < 4 else 2
+            rr = gpu.rr_counts(x, 1, emb, thr, norm)
+            np.testing.assert_array_equal(rr, oracle_mod.rr_counts(x, 1, emb, thr, norm),
+                                          err_msg=name)
+            det = gpu.det_histograms(x, 1, emb, thr, norm)
+            lam = gpu.lam_histograms(x, 1, emb, thr, norm)
+            for k, t in enumerate(thr):
+                np.testing.assert_array_equal(
+                    det[k], oracle_mod.det_hist(x, 1, emb, t, norm), err_msg=f"{name} DET {t}")
+                np.testing.assert_array_equal(
+                    lam[k], oracle_mod.lam_hist(x, 1, emb, t, norm), err_msg=f"{name} LAM {t}")
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_rp_matches_oracle(gpu, oracle_mod, dt):
+    x = workloads.lorenz_x(600, 3, transient=500).astype(dt)
+    for norm in NORMS:
+        for (tau, emb, t) in [(1, 3, 0.3), (2, 4, 0.8), (5, 1, 0.0)]:
+            got = gpu.rp(x, tau, emb, t, norm)
+            np.testing.assert_array_equal(got, oracle_mod.rp(x, tau, emb, t, norm))
+    x64 = x.astype(np.float64)
+    np.testing.assert_array_equal(gpu.rp(x64, 2, 3, 0.5, 1, out_dtype=np.int32),
+                                  oracle_mod.rp_i32(x64, 2, 3, 0.5, 1))

@@ -52,6 +52,9 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.accrqa_gb300_last_error.restype = ctypes.c_char_p
     lib.accrqa_gb300_version.restype = ctypes.c_int
     lib.accrqa_gb300_device_count.restype = ctypes.c_int
+    lib.accrqa_gb300_kernel_launches.restype = ctypes.c_uint64
+    lib.accrqa_gb300_transfer_stats.argtypes = [vp, vp, i32]
+    lib.accrqa_gb300_transfer_stats.restype = None
     lib.accrqa_gb300_threshold_keys.argtypes = [c_u64p, vp, i32, i32, i32]
     for name in ("accrqa_gb300_rr_counts", "accrqa_gb300_det_histograms",
                  "accrqa_gb300_lam_histograms"):

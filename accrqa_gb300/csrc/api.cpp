@@ -202,6 +202,12 @@ const char *accrqa_gb300_last_error(void) { return last_error(); }
 
 int accrqa_gb300_version(void) { return 10000; }
 
+void accrqa_gb300_transfer_stats(uint64_t *h2d_bytes, uint64_t *d2h_bytes, int32_t reset) {
+    transfer_stats(h2d_bytes, d2h_bytes, reset);
+}
+
+uint64_t accrqa_gb300_kernel_launches(void) { return accrqa_gb300_launch_count(); }
+
 int accrqa_gb300_device_count(void) {
     int n = 0;
     if (cudaGetDeviceCount(&n) != cudaSuccess) {

@@ -1,6 +1,7 @@
 // engine.cpp -- host side of the GB300 RQA engine (see engine.hpp).
 #include "engine.hpp"
 
+#include <atomic>
 #include <cfloat>
 #include <cmath>
 #include <cstdarg>
@@ -39,6 +40,34 @@ Accrqa_Error cuda_error(cudaError_t e, const char *what) {
         cudaError_t e_ = (call);                           \
         if (e_ != cudaSuccess) return cuda_error(e_, what); \
     } while (0)
+
+// ===========================================================================
+// Host<->device traffic accounting
+// ===========================================================================
+static std::atomic<unsigned long long> g_h2d{0}, g_d2h{0};
+
+static cudaError_t copy_async(void *dst, const void *src, size_t bytes, cudaMemcpyKind k,
+                              cudaStream_t st) {
+    if (k == cudaMemcpyHostToDevice) g_h2d.fetch_add(bytes);
+    else if (k == cudaMemcpyDeviceToHost) g_d2h.fetch_add(bytes);
+    return copy_async(dst, src, bytes, k, st);
+}
+
+static cudaError_t copy2d_d2h_async(void *dst, size_t dpitch, const void *src, size_t spitch,
+                                    size_t width, size_t height, cudaStream_t st) {
+    g_d2h.fetch_add(width * height);
+    return cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, height, cudaMemcpyDeviceToHost,
+                             st);
+}
+
+void transfer_stats(uint64_t *h2d, uint64_t *d2h, int reset) {
+    if (h2d) *h2d = g_h2d.load();
+    if (d2h) *d2h = g_d2h.load();
+    if (reset) {
+        g_h2d.store(0);
+        g_d2h.store(0);
+    }
+}
 
 // ===========================================================================
 // Device memory and contexts
@@ -342,7 +371,7 @@ template <typename T>
 static Accrqa_Error upload_series(Context &c, const T *x, int64_t n, const T **d_x) {
     const size_t bytes = (size_t)(n + ACCRQA_SERIES_PAD) * sizeof(T);
     CU(c.series.reserve(bytes), "cudaMalloc(series)");
-    CU(cudaMemcpyAsync(c.series.ptr, x, (size_t)n * sizeof(T), cudaMemcpyHostToDevice,
+    CU(copy_async(c.series.ptr, x, (size_t)n * sizeof(T), cudaMemcpyHostToDevice,
                        c.stream), "cudaMemcpy(series H2D)");
     CU(cudaMemsetAsync((T *)c.series.ptr + n, 0, ACCRQA_SERIES_PAD * sizeof(T), c.stream),
        "cudaMemset(series pad)");
@@ -396,7 +425,7 @@ static Accrqa_Error fetch_histograms(Context &c, int kind, const uint64_t *d_his
                                      int nthr, int64_t nc,
                                      std::vector<LineHistogram> &out) {
     std::vector<uint32_t> maxlen((size_t)nthr);
-    CU(cudaMemcpyAsync(maxlen.data(), d_maxlen, (size_t)nthr * 4, cudaMemcpyDeviceToHost,
+    CU(copy_async(maxlen.data(), d_maxlen, (size_t)nthr * 4, cudaMemcpyDeviceToHost,
                        c.stream), "cudaMemcpy(maxlen D2H)");
     CU(cudaStreamSynchronize(c.stream), "line kernels");
     uint32_t mx = 0;
@@ -404,8 +433,8 @@ static Accrqa_Error fetch_histograms(Context &c, int kind, const uint64_t *d_his
     int64_t p = (int64_t)(mx + 1 > ACCRQA_SHORT_RUN_BINS ? mx + 1 : ACCRQA_SHORT_RUN_BINS);
     if (p > nc + 1) p = nc + 1;
     std::vector<uint64_t> buf((size_t)p * nthr);
-    CU(cudaMemcpy2DAsync(buf.data(), (size_t)p * 8, d_hist, (size_t)stride * 8,
-                         (size_t)p * 8, (size_t)nthr, cudaMemcpyDeviceToHost, c.stream),
+    CU(copy2d_d2h_async(buf.data(), (size_t)p * 8, d_hist, (size_t)stride * 8,
+                        (size_t)p * 8, (size_t)nthr, c.stream),
        "cudaMemcpy(histogram D2H)");
     CU(cudaStreamSynchronize(c.stream), "histogram copy");
     out.clear();
@@ -454,7 +483,7 @@ Accrqa_Error run_rr(T *out, const T *x, size_t n, const int *taus, int ntau,
                 return err;
         }
     std::vector<uint64_t> counts(ncnt);
-    CU(cudaMemcpyAsync(counts.data(), d_counts, ncnt * 8, cudaMemcpyDeviceToHost, c->stream),
+    CU(copy_async(counts.data(), d_counts, ncnt * 8, cudaMemcpyDeviceToHost, c->stream),
        "cudaMemcpy(counts D2H)");
     CU(cudaStreamSynchronize(c->stream), "RR kernels");
     for (int a = 0; a < ntau; a++)
@@ -589,7 +618,7 @@ Accrqa_Error run_rp(OUT *out, const T *x, size_t n, int tau, int emb, T thr, int
                                        c->rp[0].ptr, sizeof(OUT) == 1 ? 1 : 2, r0, nr,
                                        c->stream);
         if (e) return cuda_error((cudaError_t)e, "RP kernel launch");
-        CU(cudaMemcpyAsync(out + r0 * nc, c->rp[0].ptr, (size_t)nr * row_bytes,
+        CU(copy_async(out + r0 * nc, c->rp[0].ptr, (size_t)nr * row_bytes,
                            cudaMemcpyDeviceToHost, c->stream), "cudaMemcpy(RP D2H)");
         CU(cudaStreamSynchronize(c->stream), "RP kernel");
     }
@@ -617,7 +646,7 @@ Accrqa_Error raw_rr_counts(uint64_t *counts, const T *x, int64_t n, int tau, int
     if ((err = enqueue_rr<T>(d_x, n, tau, emb, thr, nthr, norm, (uint64_t *)c->counts.ptr,
                              c->stream)))
         return err;
-    CU(cudaMemcpyAsync(counts, c->counts.ptr, (size_t)nthr * 8, cudaMemcpyDeviceToHost,
+    CU(copy_async(counts, c->counts.ptr, (size_t)nthr * 8, cudaMemcpyDeviceToHost,
                        c->stream), "cudaMemcpy(counts D2H)");
     CU(cudaStreamSynchronize(c->stream), "RR kernels");
     return SUCCESS;
@@ -649,7 +678,7 @@ Accrqa_Error raw_histograms(int kind, uint64_t *hist, const T *x, int64_t n, int
                                 (uint64_t *)c->hist.ptr, nc + 1, (uint32_t *)c->maxlen.ptr,
                                 c->stream)))
         return err;
-    CU(cudaMemcpyAsync(hist, c->hist.ptr, bytes, cudaMemcpyDeviceToHost, c->stream),
+    CU(copy_async(hist, c->hist.ptr, bytes, cudaMemcpyDeviceToHost, c->stream),
        "cudaMemcpy(histograms D2H)");
     CU(cudaStreamSynchronize(c->stream), "line kernels");
     if (kind == ACCRQA_WALK_DET) {

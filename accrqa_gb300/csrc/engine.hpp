@@ -23,6 +23,9 @@ typedef unsigned long long u64;
 void set_last_error(const char *fmt, ...);
 const char *last_error();
 Accrqa_Error cuda_error(cudaError_t e, const char *what);
+// Bytes copied host->device and device->host by the engine since load (or
+// since the last reset).
+void transfer_stats(uint64_t *h2d, uint64_t *d2h, int reset);
 
 // ---- device memory --------------------------------------------------------
 // Grow-only device allocation owned by a context.

@@ -54,6 +54,9 @@ int accrqa_gb300_launch_rp(const void *d_x, int32_t dtype, int32_t norm,
 /* Number of streaming multiprocessors of the current device (cached). */
 int accrqa_gb300_sm_count(void);
 
+/* Kernels this library has launched since it was loaded. */
+uint64_t accrqa_gb300_launch_count(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -2,12 +2,17 @@
 // (declared in engine_abi.h) and the recurrence-plot kernels.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <mutex>
 
 #include "engine_abi.h"
 #include "rqa_kernels.cuh"
 
 namespace accrqa {
+
+// Kernels launched by this library since load (reported to callers that
+// account for their GPU work, e.g. the benchmark).
+std::atomic<unsigned long long> g_launches{0};
 
 cudaError_t launch_rr_f32(const accrqa_walk_desc &, cudaStream_t);
 cudaError_t launch_rr_f64(const accrqa_walk_desc &, cudaStream_t);
@@ -49,12 +54,15 @@ static cudaError_t launch_rp_t(const void *d_x, int norm, long long nc, int tau,
             x, nc, tau, emb, key, (OUT *)d_out, row0, nrows);
     else
         return cudaErrorInvalidValue;
+    g_launches.fetch_add(1);
     return cudaGetLastError();
 }
 
 }  // namespace accrqa
 
 extern "C" int accrqa_gb300_sm_count(void) { return accrqa::sm_count_cached(); }
+
+extern "C" uint64_t accrqa_gb300_launch_count(void) { return accrqa::g_launches.load(); }
 
 extern "C" int accrqa_gb300_launch_walk(const accrqa_walk_desc *d, void *stream) {
     using namespace accrqa;

@@ -5,12 +5,15 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "engine_abi.h"
 #include "rqa_kernels.cuh"
 
 namespace accrqa {
 
 int sm_count_cached();
+extern std::atomic<unsigned long long> g_launches;
 
 template <int KIND, typename T, int NORM, int EMB, int NT>
 static cudaError_t launch_one(const accrqa_walk_desc &d, cudaStream_t st) {
@@ -61,6 +64,7 @@ static cudaError_t launch_one(const accrqa_walk_desc &d, cudaStream_t st) {
     long long cap = (long long)sm_count_cached() * per_sm;
     int grid = (int)(want < cap ? want : cap);
     kern<<<grid, kWarpsPerCta * 32, smem, st>>>(a);
+    g_launches.fetch_add(1);
     return cudaGetLastError();
 }
 

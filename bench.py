@@ -1,0 +1,447 @@
+"""Benchmark of the GB300 RQA engine on the Lorenz workload.
+
+Workload (one "step"): the x-component of the Lorenz system, N = 200,000
+samples, float32, z-scored; tau in {1,2,4,8} x emb in {3,5,8}; 16 thresholds
+0.05..0.8 (in units of the series' std); Euclidean norm; RR, DET (lmin=2) and
+LAM (vmin=2) for every (tau, emb).  Metric: recurrence-matrix cells per
+second per threshold, sum over measures of nc^2 * nthr / time.
+
+  value : device-resident passes through the engine's C ABI
+          (accrqa_gb300_*_dev), inputs already in HBM, outputs zeroed inside
+          the step; CUDA events on the launching stream.
+  e2e   : the reference-facing calls RR / DET / LAM (py_accrqa_* on host
+          numpy buffers): H2D of the series, kernels, D2H, post-processing.
+  --impl reference : the reference algorithm's CPU implementation (the
+          oracle port, OpenMP on all host cores) on a bounded sample of the
+          same workload, extrapolated to the full workload.
+
+Multi-GPU: replicas only -- every rank runs the whole workload on its own GPU
+(weak scaling); value = cells of all ranks / max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+TAUS = [1, 2, 4, 8]
+EMBS = [3, 5, 8]
+NTHR = 16
+N = 200_000
+SEED = 2024
+METRIC = "RM cells/s per threshold (RR+DET+LAM)"
+WORKLOAD = ("lorenz-x N=200000 fp32 z-scored, tau{1,2,4,8} x emb{3,5,8}, 16 thresholds "
+            "0.05-0.8 std, Euclidean, RR+DET(lmin=2)+LAM(vmin=2)")
+
+
+def series():
+    from accrqa_gb300 import workloads
+    x = workloads.lorenz_x(N, SEED).astype(np.float32)
+    thr = (np.linspace(0.05, 0.8, NTHR) * float(np.std(x.astype(np.float64)))).astype(np.float32)
+    return x, thr
+
+
+def combos():
+    return [(t, e) for t in TAUS for e in EMBS]
+
+
+def cells_per_step(measures=3):
+    tot = 0
+    for t, e in combos():
+        nc = N - (e - 1) * t
+        tot += nc * nc * NTHR
+    return tot * measures
+
+
+def algo_ops(nc, emb, nthr):
+    """FP32 operations one pass performs by the algorithm's count:
+    U * (3*emb + 1 + nthr), U = nc(nc+1)/2 unique pairs (sub, mul, add per
+    dimension, one sqrt, one compare per threshold)."""
+    u = nc * (nc + 1) // 2
+    return u * (3 * emb + 1 + nthr)
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [v.strip() for v in ln.split(",")]
+            if len(p) < 7:
+                continue
+            try:
+                sm.append(float(p[0]))
+                mx.append(float(p[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    import accrqa_gb300
+    from accrqa_gb300 import _lib, engine
+
+    ws, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        dist.init_process_group("nccl")
+    lib = _lib.handle()
+    dev = torch.device("cuda", local)
+    x, thr = series()
+    stream = torch.cuda.current_stream(dev)
+    sp = stream.cuda_stream
+
+    # device-resident inputs and outputs
+    dx = torch.zeros(N + 128, dtype=torch.float32, device=dev)
+    dx[:N].copy_(torch.from_numpy(x))
+    layout, off = [], 0
+    for t, e in combos():
+        nc = N - (e - 1) * t
+        layout.append((t, e, nc, off))
+        off += NTHR * (nc + 1)
+    d_det = torch.zeros(off, dtype=torch.int64, device=dev)
+    d_lam = torch.zeros(off, dtype=torch.int64, device=dev)
+    d_cnt = torch.zeros(len(layout) * NTHR, dtype=torch.int64, device=dev)
+    d_max = torch.zeros(2 * len(layout) * NTHR, dtype=torch.int32, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)   # > 129 MB L2
+
+    kinds = ("rr", "det", "lam")
+    ev = {k: [] for k in kinds}
+
+    def step(record):
+        d_det.zero_()
+        d_lam.zero_()
+        d_cnt.zero_()
+        d_max.zero_()
+        for ci, (t, e, nc, o) in enumerate(layout):
+            for kind in kinds:
+                if record:
+                    s0 = torch.cuda.Event(enable_timing=True)
+                    s0.record(stream)
+                if kind == "rr":
+                    engine.rr_counts_dev(d_cnt.data_ptr() + ci * NTHR * 8, dx.data_ptr(),
+                                         engine.F32, N, t, e, thr, 1, sp)
+                elif kind == "det":
+                    engine.det_hist_dev(d_det.data_ptr() + o * 8, nc + 1,
+                                        d_max.data_ptr() + ci * NTHR * 4, dx.data_ptr(),
+                                        engine.F32, N, t, e, thr, 1, sp)
+                else:
+                    engine.lam_hist_dev(d_lam.data_ptr() + o * 8, nc + 1,
+                                        d_max.data_ptr() + (len(layout) + ci) * NTHR * 4,
+                                        dx.data_ptr(), engine.F32, N, t, e, thr, 1, sp)
+                if record:
+                    s1 = torch.cuda.Event(enable_timing=True)
+                    s1.record(stream)
+                    ev[kind].append((s0, s1, nc, e))
+
+    for _ in range(args.warmup):
+        step(False)
+    torch.cuda.synchronize()
+    if ws > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = lib.accrqa_gb300_kernel_launches()
+    step_ms = []
+    for _ in range(args.steps):
+        flush.fill_(1)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        step(True)
+        b.record(stream)
+        b.synchronize()
+        step_ms.append(a.elapsed_time(b))
+    torch.cuda.synchronize()
+    launches = lib.accrqa_gb300_kernel_launches() - launches0
+    clk = clocks.stop()
+    total_ms = float(sum(step_ms))
+    if ws > 1:
+        tt = torch.tensor([total_ms], device=dev, dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        total_ms = float(tt.item())
+        dist.barrier()
+
+    # per-kernel totals and the dominant kernel's roofline
+    per_kind = {}
+    for kind in kinds:
+        ms = sum(s0.elapsed_time(s1) for s0, s1, _, _ in ev[kind])
+        ops = sum(algo_ops(nc, e, NTHR) for _, _, nc, e in ev[kind])
+        per_kind[kind] = {"ms": ms, "ops": ops, "launches": len(ev[kind])}
+    dom = max(per_kind, key=lambda k: per_kind[k]["ms"])
+    props = torch.cuda.get_device_properties(dev)
+    sm_mhz = clk.get("sm_mhz") or 1462.0
+    peak_ops = props.multi_processor_count * 128 * sm_mhz * 1e6   # non-FMA FP32 issue rate
+    achieved = per_kind[dom]["ops"] / (per_kind[dom]["ms"] * 1e-3)
+
+    # end to end through the reference-facing API (host buffers)
+    taus = np.array(TAUS, dtype=np.intc)
+    embs = np.array(EMBS, dtype=np.intc)
+    lm = np.array([2], dtype=np.intc)
+    D = accrqa_gb300.accrqaDistance("euclidean")
+    e2e_steps = max(1, min(args.steps, 3))
+
+    def e2e_step():
+        accrqa_gb300.RR(x, taus, embs, thr, D, tidy_data=False)
+        accrqa_gb300.DET(x, taus, embs, lm, thr, D, tidy_data=False)
+        accrqa_gb300.LAM(x, taus, embs, lm, thr, D, tidy_data=False)
+
+    e2e_step()   # warm-up
+    torch.cuda.synchronize()
+    if ws > 1:
+        dist.barrier()
+    lib.accrqa_gb300_transfer_stats(None, None, 1)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        e2e_step()
+    e2e_s = time.perf_counter() - t0
+    import ctypes
+    h2d, d2h = ctypes.c_uint64(), ctypes.c_uint64()
+    lib.accrqa_gb300_transfer_stats(ctypes.byref(h2d), ctypes.byref(d2h), 0)
+    if ws > 1:
+        tt = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+
+    cells = cells_per_step() * args.steps * ws
+    value = cells / (total_ms * 1e-3)
+    e2e_value = cells_per_step() * e2e_steps * ws / e2e_s
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "cells/s",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "parallelism": f"replicas{ws}",
+                   "l2": "flushed by a 256 MB write before every timed step",
+                   "inputs_in_hbm": True},
+        "e2e": {"value": e2e_value, "unit": "cells/s",
+                "h2d_bytes_per_step": int(h2d.value // e2e_steps),
+                "d2h_bytes_per_step": int(d2h.value // e2e_steps),
+                "path": "accrqa_gb300.RR/DET/LAM -> py_accrqa_* (host numpy buffers)"},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "fp32", "kernel": dom, "achieved": achieved / 1e12,
+                     "peak": peak_ops / 1e12, "unit": "TFLOP/s",
+                     "frac": achieved / peak_ops, "traffic": None,
+                     "peak_source": f"derived: {props.multi_processor_count} SMs x 128 FP32 "
+                                    f"lanes x {sm_mhz:.0f} MHz median SM clock under load",
+                     "ops_per_launch": "U*(3*emb+1+nthr), U=nc(nc+1)/2"},
+        "kernels": {k: {"ms_total": v["ms"], "launches": v["launches"],
+                        "tflops_algorithmic": v["ops"] / (v["ms"] * 1e-3) / 1e12}
+                    for k, v in per_kind.items()},
+        "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        dist.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline (the oracle port, test infrastructure; timed, never shipped)
+# ---------------------------------------------------------------------------
+def cpu_sample(budget_s):
+    """Time RR, DET and LAM of the reference algorithm (one threshold, tau=1)
+    for each emb of the workload, each on a bounded slice at full N (rows of
+    the full matrix for RR and LAM, diagonals for DET), and extrapolate the
+    measured cost per cell to every (tau, emb, threshold, measure)."""
+    from oracle import oracle
+    x, thr = series()
+    t = float(thr[NTHR // 2])
+    per = budget_s / (3.0 * len(EMBS))
+    rate = {}
+    cells_done = 0
+    for emb in EMBS:
+        nc = N - (emb - 1)
+        for kind in ("rr", "lam", "det"):
+            span, pos, spent, cells = 16, 1 if kind == "det" else 0, 0.0, 0
+            while spent < per:
+                t0 = time.perf_counter()
+                if kind == "rr":
+                    _, c = oracle.rr_sample(x, 1, emb, t, 1, pos, pos + span)
+                elif kind == "lam":
+                    _, _, c = oracle.lam_sample(x, 1, emb, t, 1, pos, pos + span)
+                else:
+                    _, c = oracle.det_sample(x, 1, emb, t, 1, pos, pos + span)
+                dt = time.perf_counter() - t0
+                spent += dt
+                cells += c
+                pos += span
+                if dt < per / 4:
+                    span *= 2
+            rate[(kind, emb)] = cells / spent
+            cells_done += cells
+    est = 0.0
+    for tt, e in combos():
+        ncc = N - (e - 1) * tt
+        est += NTHR * (ncc * ncc / rate[("rr", e)] + ncc * ncc / rate[("lam", e)]
+                       + ncc * (ncc - 1) / 2 / rate[("det", e)])
+    return cells_per_step() / est, cells_done, oracle.num_threads()
+
+
+def cpu_baseline(budget_s):
+    t0 = time.perf_counter()
+    value, cells, cores = cpu_sample(budget_s)
+    return {"value": value, "unit": "cells/s", "cores": cores, "kind": "port",
+            "sample": f"{cells:.3g} cells in {time.perf_counter() - t0:.1f}s: full N, tau=1, "
+                      "1 threshold, row slices (RR, LAM) and diagonal slices (DET) for each "
+                      "emb in {3,5,8}; cost per cell extrapolated to every (tau, emb, "
+                      "threshold, measure) of the workload"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_setup()
+    if rank != 0:
+        return
+    from oracle import oracle
+    oracle.build()
+    vals, ms = [], []
+    budget = args.cpu_seconds
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        v, _, cores = cpu_sample(budget / 2 if i < args.warmup else budget)
+        if i >= args.warmup:
+            vals.append(v)
+            ms.append((time.perf_counter() - t0) * 1e3)
+    value = statistics.median(vals)
+    line = {
+        "metric": METRIC, "value": value, "unit": "cells/s", "impl": "reference",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": statistics.mean(ms), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "parallelism": "cpu"},
+        "cpu_baseline": {"value": value, "unit": "cells/s", "cores": cores, "kind": "port",
+                         "sample": "per step: tau=1 emb=3 full N, 1 threshold, bounded "
+                                   "row/diagonal slices of RR, DET, LAM, extrapolated"},
+        "e2e": {"value": value, "unit": "cells/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_case(args):
+    """One pass of one kernel on a smaller series (for profiler captures):
+    --case rr|det|lam, --n samples, tau=1, emb=5, 16 thresholds."""
+    import torch
+
+    from accrqa_gb300 import engine
+    from accrqa_gb300 import workloads
+    n = args.n
+    x = workloads.lorenz_x(n, SEED).astype(np.float32)
+    thr = (np.linspace(0.05, 0.8, NTHR) * float(np.std(x.astype(np.float64)))).astype(np.float32)
+    dev = torch.device("cuda", 0)
+    sp = torch.cuda.current_stream(dev).cuda_stream
+    dx = torch.zeros(n + 128, dtype=torch.float32, device=dev)
+    dx[:n].copy_(torch.from_numpy(x))
+    tau, emb = 1, 5
+    nc = n - (emb - 1) * tau
+    hist = torch.zeros(NTHR * (nc + 1), dtype=torch.int64, device=dev)
+    cnt = torch.zeros(NTHR, dtype=torch.int64, device=dev)
+    mx = torch.zeros(NTHR, dtype=torch.int32, device=dev)
+    for _ in range(args.warmup + args.steps):
+        hist.zero_()
+        cnt.zero_()
+        if args.case == "rr":
+            engine.rr_counts_dev(cnt.data_ptr(), dx.data_ptr(), engine.F32, n, tau, emb, thr,
+                                 1, sp)
+        elif args.case == "det":
+            engine.det_hist_dev(hist.data_ptr(), nc + 1, mx.data_ptr(), dx.data_ptr(),
+                                engine.F32, n, tau, emb, thr, 1, sp)
+        else:
+            engine.lam_hist_dev(hist.data_ptr(), nc + 1, mx.data_ptr(), dx.data_ptr(),
+                                engine.F32, n, tau, emb, thr, 1, sp)
+    torch.cuda.synchronize()
+    print(json.dumps({"case": args.case, "n": n, "done": True}))
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--case", choices=["rr", "det", "lam"], default=None,
+                    help="run a single pass of one kernel (profiling)")
+    ap.add_argument("--n", type=int, default=50_000)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args(argv)
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    if args.case:
+        run_case(args)
+    elif args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -186,6 +186,14 @@ int accrqa_gb300_version(void);
 /* Number of CUDA devices visible (0 when none or no driver). */
 int accrqa_gb300_device_count(void);
 
+/* Bytes the engine has copied host->device and device->host since load, or
+ * since the last call with reset != 0. */
+void accrqa_gb300_transfer_stats(uint64_t *h2d_bytes, uint64_t *d2h_bytes,
+                                 int32_t reset);
+
+/* Number of CUDA kernels the engine has launched since load. */
+uint64_t accrqa_gb300_kernel_launches(void);
+
 /* Comparison keys the kernels use for `nthr` thresholds of dtype `dtype`
  * under norm `norm` (1 Euclidean, 2 maximal): keys[k] is the largest value
  * v >= +0 of the squared sum (Euclidean) or of the maximal distance for which

@@ -359,3 +359,26 @@ void oracle_set_threads(int n) {
     (void)n;
 #endif
 }
+
+/* Timed CPU-baseline kernel for RR: recurrent cells of rows [r_begin, r_end)
+ * of the full matrix for one threshold (src/AccRQA_CPU_function.cpp:347-378
+ * restricted to a row range).  Returns the cells visited; *count gets the
+ * recurrent ones. */
+#define DEFINE_RR_SAMPLE(T, SUF)                                               \
+    u64 oracle_rr_sample_##SUF(u64 *count, const T *x, int64_t n, int tau,    \
+                               int emb, T thr, int dist, int64_t r_begin,      \
+                               int64_t r_end) {                                \
+        int64_t nc = n - (int64_t)(emb - 1) * tau;                             \
+        u64 ones = 0;                                                          \
+        if (r_begin < 0) r_begin = 0;                                          \
+        if (r_end > nc) r_end = nc;                                            \
+        if (r_end <= r_begin) return 0;                                        \
+        _Pragma("omp parallel for reduction(+:ones) schedule(dynamic, 4)")     \
+        for (int64_t i = r_begin; i < r_end; i++)                              \
+            for (int64_t j = 0; j < nc; j++)                                   \
+                ones += (u64)rec_##SUF(x, i, j, thr, tau, emb, dist);          \
+        *count = ones;                                                         \
+        return (u64)(r_end - r_begin) * (u64)nc;                               \
+    }
+DEFINE_RR_SAMPLE(float, f32)
+DEFINE_RR_SAMPLE(double, f64)

@@ -155,6 +155,19 @@ def det_sample(x, tau, emb, threshold, dist, d_begin, d_end):
     return out, int(cells)
 
 
+def rr_sample(x, tau, emb, threshold, dist, r_begin, r_end):
+    """Recurrent cells of rows [r_begin, r_end); returns (count, cells)."""
+    x = np.ascontiguousarray(x)
+    suf, ct = _suffix(x)
+    cnt = np.zeros(1, dtype=np.uint64)
+    fn = getattr(lib(), "oracle_rr_sample_" + suf)
+    fn.restype = ctypes.c_uint64
+    cells = fn(_ptr(cnt, ctypes.c_uint64), _ptr(x, ct), _i64(len(x)), ctypes.c_int(tau),
+               ctypes.c_int(emb), ct(float(threshold)), ctypes.c_int(dist), _i64(r_begin),
+               _i64(r_end))
+    return int(cnt[0]), int(cells)
+
+
 def lam_sample(x, tau, emb, threshold, dist, r_begin, r_end):
     """LAM run histogram + recurrent count over rows [r_begin, r_end)."""
     x = np.ascontiguousarray(x)

@@ -126,6 +126,14 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+_T0 = time.perf_counter()
+
+
+def log(msg):
+    """Progress line on stderr (the JSON result goes to stdout)."""
+    print(f"[bench {time.perf_counter() - _T0:7.1f}s] {msg}", file=sys.stderr, flush=True)
+
+
 def dist_setup():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -196,8 +204,11 @@ def run_ours(args):
                     s1.record(stream)
                     ev[kind].append((s0, s1, nc, e))
 
+    log("inputs ready; warm-up")
     for _ in range(args.warmup):
         step(False)
+        torch.cuda.synchronize()
+        log("warm-up step done")
     torch.cuda.synchronize()
     if ws > 1:
         dist.barrier()
@@ -215,6 +226,7 @@ def run_ours(args):
         b.record(stream)
         b.synchronize()
         step_ms.append(a.elapsed_time(b))
+        log(f"timed step {step_ms[-1]:.1f} ms")
     torch.cuda.synchronize()
     launches = lib.accrqa_gb300_kernel_launches() - launches0
     clk = clocks.stop()
@@ -249,8 +261,10 @@ def run_ours(args):
         accrqa_gb300.DET(x, taus, embs, lm, thr, D, tidy_data=False)
         accrqa_gb300.LAM(x, taus, embs, lm, thr, D, tidy_data=False)
 
+    log("clocks stopped; e2e warm-up")
     e2e_step()   # warm-up
     torch.cuda.synchronize()
+    log("e2e warm-up done")
     if ws > 1:
         dist.barrier()
     lib.accrqa_gb300_transfer_stats(None, None, 1)
@@ -260,6 +274,7 @@ def run_ours(args):
         torch.cuda.synchronize()
         e2e_step()
     e2e_s = time.perf_counter() - t0
+    log(f"e2e {e2e_s / e2e_steps:.2f} s per step")
     import ctypes
     h2d, d2h = ctypes.c_uint64(), ctypes.c_uint64()
     lib.accrqa_gb300_transfer_stats(ctypes.byref(h2d), ctypes.byref(d2h), 0)
@@ -297,7 +312,9 @@ def run_ours(args):
         "clocks": clk,
     }
     if rank == 0 and not args.no_cpu_baseline:
+        log("cpu baseline")
         line["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
+        log("cpu baseline done")
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:

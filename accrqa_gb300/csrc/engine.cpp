@@ -3,6 +3,8 @@
 
 #include <atomic>
 #include <cfloat>
+#include <chrono>
+#include <cstdlib>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -25,6 +27,28 @@ void set_last_error(const char *fmt, ...) {
 }
 
 const char *last_error() { return g_last_error; }
+
+// Host-side phase trace on stderr, enabled by ACCRQA_GB300_TRACE=1.
+static bool trace_on() {
+    static const bool on = [] {
+        const char *v = std::getenv("ACCRQA_GB300_TRACE");
+        return v && v[0] == '1';
+    }();
+    return on;
+}
+
+static void trace(const char *fmt, ...) {
+    if (!trace_on()) return;
+    static const auto t0 = std::chrono::steady_clock::now();
+    const double ms = std::chrono::duration<double, std::milli>(
+                          std::chrono::steady_clock::now() - t0).count();
+    std::fprintf(stderr, "[accrqa %10.3f ms] ", ms);
+    va_list ap;
+    va_start(ap, fmt);
+    std::vfprintf(stderr, fmt, ap);
+    va_end(ap);
+    std::fputc('\n', stderr);
+}
 
 Accrqa_Error cuda_error(cudaError_t e, const char *what) {
     set_last_error("%s: %s", what, cudaGetErrorString(e));
@@ -428,6 +452,7 @@ static Accrqa_Error fetch_histograms(Context &c, int kind, const uint64_t *d_his
     CU(copy_async(maxlen.data(), d_maxlen, (size_t)nthr * 4, cudaMemcpyDeviceToHost,
                        c.stream), "cudaMemcpy(maxlen D2H)");
     CU(cudaStreamSynchronize(c.stream), "line kernels");
+    trace("fetch: kernels done (nc=%lld)", (long long)nc);
     uint32_t mx = 0;
     for (uint32_t v : maxlen) mx = v > mx ? v : mx;
     int64_t p = (int64_t)(mx + 1 > ACCRQA_SHORT_RUN_BINS ? mx + 1 : ACCRQA_SHORT_RUN_BINS);
@@ -437,6 +462,7 @@ static Accrqa_Error fetch_histograms(Context &c, int kind, const uint64_t *d_his
                         (size_t)p * 8, (size_t)nthr, c.stream),
        "cudaMemcpy(histogram D2H)");
     CU(cudaStreamSynchronize(c.stream), "histogram copy");
+    trace("fetch: %lld bins x %d thresholds copied", (long long)p, nthr);
     out.clear();
     out.reserve((size_t)nthr);
     for (int k = 0; k < nthr; k++) {
@@ -451,6 +477,7 @@ static Accrqa_Error fetch_histograms(Context &c, int kind, const uint64_t *d_his
         }
         out.emplace_back(std::move(h), last, nc);
     }
+    trace("fetch: histograms wrapped");
     return SUCCESS;
 }
 
@@ -482,10 +509,12 @@ Accrqa_Error run_rr(T *out, const T *x, size_t n, const int *taus, int ntau,
                                      dst, c->stream)))
                 return err;
         }
+    trace("RR: %d passes enqueued", ntau * nemb);
     std::vector<uint64_t> counts(ncnt);
     CU(copy_async(counts.data(), d_counts, ncnt * 8, cudaMemcpyDeviceToHost, c->stream),
        "cudaMemcpy(counts D2H)");
     CU(cudaStreamSynchronize(c->stream), "RR kernels");
+    trace("RR: kernels done");
     for (int a = 0; a < ntau; a++)
         for (int b = 0; b < nemb; b++) {
             const int64_t nc = embedded_length(n, taus[a], embs[b]);
@@ -558,6 +587,7 @@ Accrqa_Error run_lines(int kind, T *out, const T *x, size_t n, const int *taus,
                                         d_max + (size_t)(q - first) * nthr, c->stream)))
                 return err;
         }
+        trace("lines: batch [%d, %d) enqueued", first, last);
         for (int q = first; q < last; q++) {
             const int a = q / nemb, b = q % nemb;
             const int64_t nc = embedded_length(n, taus[a], embs[b]);
@@ -588,6 +618,7 @@ Accrqa_Error run_lines(int kind, T *out, const T *x, size_t n, const int *taus,
                     out[5 * pos + 4] = (T)rr;
                 }
             }
+            trace("lines: combo %d measures done", q);
         }
     }
     return SUCCESS;

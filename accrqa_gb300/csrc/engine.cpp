@@ -74,7 +74,7 @@ static cudaError_t copy_async(void *dst, const void *src, size_t bytes, cudaMemc
                               cudaStream_t st) {
     if (k == cudaMemcpyHostToDevice) g_h2d.fetch_add(bytes);
     else if (k == cudaMemcpyDeviceToHost) g_d2h.fetch_add(bytes);
-    return copy_async(dst, src, bytes, k, st);
+    return cudaMemcpyAsync(dst, src, bytes, k, st);
 }
 
 static cudaError_t copy2d_d2h_async(void *dst, size_t dpitch, const void *src, size_t spitch,

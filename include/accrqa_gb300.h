@@ -272,6 +272,28 @@ Accrqa_Error accrqa_gb300_lam_hist_dev(uint64_t *d_hist, int64_t stride,
                                        int32_t nthr, int32_t norm,
                                        void *stream);
 
+/* Recurrence rate for callers that cannot allocate device memory.  No
+ * counterpart in the reference: it exists for callers that may not call
+ * cudaMalloc -- code running while a stream is captured into a CUDA graph,
+ * hosts that give a plug-in a fixed memory arena, latency-bound serving
+ * loops.  The caller passes the series d_x (device, >= n + 128 elements of
+ * dtype) and the output d_rr (device, nthr values of dtype); thresholds are
+ * host values of dtype.  d_rr[k] = count_k / nc^2 as the RR path computes it.
+ * Work is enqueued on `stream`; the call returns without synchronising.
+ *   - No allocation: the per-threshold counts live in an 8 KiB scratch array
+ *     compiled into the library, which every GPU that loads the library holds
+ *     until the process exits.  At most 1024 thresholds per call; more
+ *     returns ERR_INVALID_ARGUMENT.
+ *   - The first call on each device looks up that array's device address
+ *     (cudaGetSymbolAddress); make that first call before any stream capture.
+ *   - All calls share the array and each call clears the part it uses first:
+ *     calls that overlap on the GPU race on it and must be ordered by the
+ *     caller (one stream, or events between streams). */
+Accrqa_Error accrqa_gb300_rr_dev_noalloc(void *d_rr, const void *d_x, int32_t dtype,
+                                         int64_t n, int32_t tau, int32_t emb,
+                                         const void *thresholds, int32_t nthr,
+                                         int32_t norm, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -141,6 +141,24 @@ def dist_setup():
     return ws, rank, local
 
 
+def reduce_max(value, device=None):
+    """Max of a per-rank float over the initialised process group (identity
+    without one).  Replicas only: this is the one cross-rank exchange."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(value)
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(cells_per_rank_step, steps, world_size, max_seconds):
+    """Whole-job throughput of independent replicas: every rank's cells over
+    the slowest rank's time."""
+    return cells_per_rank_step * steps * world_size / max_seconds
+
+
 # ---------------------------------------------------------------------------
 # our arm
 # ---------------------------------------------------------------------------
@@ -230,11 +248,8 @@ def run_ours(args):
     torch.cuda.synchronize()
     launches = lib.accrqa_gb300_kernel_launches() - launches0
     clk = clocks.stop()
-    total_ms = float(sum(step_ms))
+    total_ms = reduce_max(float(sum(step_ms)), dev)
     if ws > 1:
-        tt = torch.tensor([total_ms], device=dev, dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        total_ms = float(tt.item())
         dist.barrier()
 
     # per-kernel totals and the dominant kernel's roofline
@@ -278,14 +293,10 @@ def run_ours(args):
     import ctypes
     h2d, d2h = ctypes.c_uint64(), ctypes.c_uint64()
     lib.accrqa_gb300_transfer_stats(ctypes.byref(h2d), ctypes.byref(d2h), 0)
-    if ws > 1:
-        tt = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_s = float(tt.item())
+    e2e_s = reduce_max(e2e_s, dev)
 
-    cells = cells_per_step() * args.steps * ws
-    value = cells / (total_ms * 1e-3)
-    e2e_value = cells_per_step() * e2e_steps * ws / e2e_s
+    value = replica_rate(cells_per_step(), args.steps, ws, total_ms * 1e-3)
+    e2e_value = replica_rate(cells_per_step(), e2e_steps, ws, e2e_s)
 
     line = {
         "metric": METRIC, "value": value, "unit": "cells/s",

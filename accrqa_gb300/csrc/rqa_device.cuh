@@ -41,15 +41,20 @@ constexpr int kMaxThrPerPass = 16;
 constexpr int kShortRunBins = 512;
 
 // Kernel arguments, passed by value so that the threshold keys live in the
-// constant bank and every compare reads its key as an immediate operand.
+// constant bank and every compare reads its key as an operand.  Slots are
+// sorted by decreasing threshold (slot 0 = widest), so a cell recurrent at
+// slot k is recurrent at every slot below k; padding slots hold the
+// never-recurrent key and sort last.  row[k] is the caller's threshold index
+// of slot k (where its counts / histogram go).
 struct WalkArgs {
     const void *x;          // series in the input dtype (device)
     long long nc;           // embedded length n - (emb-1)*tau
     int tau;
     int emb;                // used by the generic (runtime-emb) instantiation
-    int nthr;               // thresholds in this pass (<= kMaxThrPerPass)
+    int nthr;               // real thresholds in this pass (<= kMaxThrPerPass)
     int pad_;
     u64 keys[kMaxThrPerPass];
+    int row[kMaxThrPerPass];
     u64 *counts;            // [nthr] recurrent-cell counts (RR)
     u64 *hist;              // [nthr][hist_stride] line-length histograms
     long long hist_stride;
@@ -101,22 +106,54 @@ __device__ __forceinline__ bool is_rec(double v, u64 key) {
     return (u64)__double_as_longlong(v) < key;
 }
 
+// Append one cell to every slot's mask: masks are shifted left and the new
+// cell enters at bit 0 as 1 when it is NOT recurrent.
+//   float : d = key - v on the FMA pipe; its sign bit is the answer (v <= key
+//           gives +0 or a positive d; a NaN v was mapped to +inf first) and
+//           one funnel shift moves it into the mask.
+//   double: an integer compare of the bit pattern against the limit.
+template <int NT>
+__device__ __forceinline__ void push_cell(u32 (&m)[NT], float v, const u64 (&keys)[kMaxThrPerPass]) {
+    v = fminf(v, __int_as_float(0x7f800000));
+#pragma unroll
+    for (int k = 0; k < NT; k++) {
+        const float d = __fsub_rn(__uint_as_float((u32)keys[k]), v);
+        m[k] = __funnelshift_l(__float_as_uint(d), m[k], 1);
+    }
+}
+template <int NT>
+__device__ __forceinline__ void push_cell(u32 (&m)[NT], double v, const u64 (&keys)[kMaxThrPerPass]) {
+    const u64 b = (u64)__double_as_longlong(v);
+#pragma unroll
+    for (int k = 0; k < NT; k++) m[k] = (m[k] << 1) | (b >= keys[k] ? 1u : 0u);
+}
+
+// Value that is never recurrent (for cells past the end of a line).
+template <typename T> __device__ __forceinline__ T never_value();
+template <> __device__ __forceinline__ float never_value<float>() { return __int_as_float(0x7f800000); }
+template <> __device__ __forceinline__ double never_value<double>() { return __longlong_as_double(-1ll); }
+
+// Recurrent-cell mask in walk order (bit c = c-th pushed cell) from the
+// pushed "not recurrent" bits.
+__device__ __forceinline__ u32 walk_mask(u32 m) { return __brev(~m); }
+
 // ---------------------------------------------------------------------------
 // Line-length bookkeeping.  A 32-bit mask holds 32 consecutive cells of one
 // line (bit c = c-th cell in walk order); `carry` is the length of the run
 // that reached the end of the previous mask.
 // ---------------------------------------------------------------------------
 struct HistSink {
-    u32 *sh;          // shared bins [kMaxThrPerPass][kShortRunBins]
-    u32 *shmax;       // shared longest line [kMaxThrPerPass]
+    u32 *sh;          // shared bins [kMaxThrPerPass][kShortRunBins], by slot
+    u32 *shmax;       // shared longest line [kMaxThrPerPass], by slot
     u64 *gh;          // global histogram base
     long long stride;
+    const int *row;   // slot -> histogram row
 
     __device__ __forceinline__ void emit(int k, u32 len) const {
         if (len < (u32)kShortRunBins) {
             atomicAdd(&sh[k * kShortRunBins + len], 1u);
         } else {
-            atomicAdd(&gh[(long long)k * stride + len], 1ull);
+            atomicAdd(&gh[(long long)row[k] * stride + len], 1ull);
             atomicMax(&shmax[k], len);
         }
     }

@@ -98,11 +98,22 @@ __device__ __forceinline__ void hist_smem_flush(const u32 *sh, const u32 *shmax,
         u32 c = sh[t];
         if (c) {
             int k = t / kShortRunBins, l = t - k * kShortRunBins;
-            atomicAdd(&p.hist[(long long)k * p.hist_stride + l], (u64)c);
+            atomicAdd(&p.hist[(long long)p.row[k] * p.hist_stride + l], (u64)c);
         }
     }
     for (int t = threadIdx.x; t < p.nthr; t += blockDim.x)
-        if (shmax[t]) atomicMax(&p.maxlen[t], shmax[t]);
+        if (shmax[t]) atomicMax(&p.maxlen[p.row[t]], shmax[t]);
+}
+
+// Close the runs of one 32-cell block for every slot.  Slots nest (slot 0 is
+// the widest threshold), so when slot 0 has neither a recurrent cell nor an
+// open run, no slot has one and the block needs no work.
+template <int NT>
+__device__ __forceinline__ void close_block(const u32 (&m)[NT], u32 (&carry)[NT],
+                                            const HistSink &sink) {
+    if ((walk_mask(m[0]) | carry[0]) == 0u) return;
+#pragma unroll
+    for (int k = 0; k < NT; k++) runs_of_mask(walk_mask(m[k]), carry[k], k, sink);
 }
 
 // ---------------------------------------------------------------------------
@@ -119,8 +130,8 @@ rr_rows(const __grid_constant__ WalkArgs p) {
     const long long nc = p.nc;
     const long long tau = p.tau;
 
-    // Lane k keeps the 64-bit total of threshold k; per-band lane counters
-    // are 32-bit (a band walk adds at most nc per lane).
+    // Lane k keeps the 64-bit total of slot k; per-band lane counters are
+    // 32-bit (a band walk adds at most nc per lane).
     u64 total = 0;
 
     for (long long unit = gwarp; unit < p.nunits; unit += nwarps) {
@@ -132,47 +143,48 @@ rr_rows(const __grid_constant__ WalkArgs p) {
             const bool row_ok = i < nc;
             T a[EMB > 0 ? EMB : 1];
             load_lane_vec<T, EMB>(a, x + i, tau);
-            u32 up[NT], dg[NT];
-#pragma unroll
-            for (int k = 0; k < NT; k++) { up[k] = 0; dg[k] = 0; }
-            // first block: contains the main diagonal; checked cell by cell
+            u32 up[NT], dg[NT], m[NT];
             {
-                const long long j0 = band * 32;
-#pragma unroll 4
-                for (int c = 0; c < 32; c++) {
-                    const long long j = j0 + c;
-                    T v = cell_dist<T, NORM, EMB>(a, x + i, x + j, tau, p.emb);
-                    const bool diag = row_ok && j == i;
-                    const bool upper = row_ok && j > i && j < nc;
+                const T v = cell_dist<T, NORM, EMB>(a, x + i, x + i, tau, p.emb);
 #pragma unroll
-                    for (int k = 0; k < NT; k++) {
-                        const bool r = is_rec(v, p.keys[k]);
-                        dg[k] += (diag && r) ? 1u : 0u;
-                        up[k] += (upper && r) ? 1u : 0u;
-                    }
+                for (int k = 0; k < NT; k++) {
+                    dg[k] = (row_ok && is_rec(v, p.keys[k])) ? 1u : 0u;
+                    up[k] = 0;
+                    m[k] = 0;
                 }
             }
-            // full blocks: j > i for every lane, all columns inside the matrix
-            long long j0 = band * 32 + 32;
-            for (; j0 + 32 <= nc; j0 += 32) {
-                const T *xj = x + j0;
-#pragma unroll 8
-                for (int c = 0; c < 32; c++) {
-                    T v = cell_dist<T, NORM, EMB>(a, x + i, xj + c, tau, p.emb);
+            // first block: the columns j > i of the diagonal tile
+            const long long j0 = band * 32;
+#pragma unroll 4
+            for (int c = 0; c < 32; c++) {
+                const long long j = j0 + c;
+                T v = cell_dist<T, NORM, EMB>(a, x + i, x + j, tau, p.emb);
+                if (!(j > i && j < nc)) v = never_value<T>();
+                push_cell<NT>(m, v, p.keys);
+            }
 #pragma unroll
-                    for (int k = 0; k < NT; k++) up[k] += is_rec(v, p.keys[k]) ? 1u : 0u;
-                }
+            for (int k = 0; k < NT; k++) up[k] += 32u - __popc(m[k]);
+            // full blocks: j > i for every lane, all columns inside the matrix
+            long long jb = j0 + 32;
+            for (; jb + 32 <= nc; jb += 32) {
+                const T *xj = x + jb;
+#pragma unroll 8
+                for (int c = 0; c < 32; c++)
+                    push_cell<NT>(m, cell_dist<T, NORM, EMB>(a, x + i, xj + c, tau, p.emb), p.keys);
+#pragma unroll
+                for (int k = 0; k < NT; k++) up[k] += 32u - __popc(m[k]);
             }
             // tail block
-            if (j0 < nc) {
+            if (jb < nc) {
 #pragma unroll 4
                 for (int c = 0; c < 32; c++) {
-                    const long long j = j0 + c;
+                    const long long j = jb + c;
                     T v = cell_dist<T, NORM, EMB>(a, x + i, x + j, tau, p.emb);
-                    const bool ok = row_ok && j < nc;
-#pragma unroll
-                    for (int k = 0; k < NT; k++) up[k] += (ok && is_rec(v, p.keys[k])) ? 1u : 0u;
+                    if (j >= nc) v = never_value<T>();
+                    push_cell<NT>(m, v, p.keys);
                 }
+#pragma unroll
+                for (int k = 0; k < NT; k++) up[k] += 32u - __popc(m[k]);
             }
 #pragma unroll
             for (int k = 0; k < NT; k++) {
@@ -183,7 +195,7 @@ rr_rows(const __grid_constant__ WalkArgs p) {
             }
         }
     }
-    if (lane < p.nthr && lane < NT && total) atomicAdd(&p.counts[lane], total);
+    if (lane < p.nthr && lane < NT && total) atomicAdd(&p.counts[p.row[lane]], total);
 }
 
 // ---------------------------------------------------------------------------
@@ -198,27 +210,16 @@ __device__ __forceinline__ void det_block(const T *__restrict__ xs,
                                           long long tau, int emb, long long rem,
                                           const WalkArgs &p, u32 (&carry)[NT],
                                           const HistSink &sink) {
-    u32 mask[NT];
+    u32 m[NT];
 #pragma unroll
-    for (int k = 0; k < NT; k++) mask[k] = 0;
-#pragma unroll 1
-    for (int g = 0; g < 32; g += 8) {
-        u32 m8[NT];
-#pragma unroll
-        for (int k = 0; k < NT; k++) m8[k] = 0;
-#pragma unroll
-        for (int c = 0; c < 8; c++) {
-            T v = cell_dist_mem<T, NORM, EMB>(xs + g + c, xsd + g + c, tau, emb);
-            const bool ok = !CHECK || (long long)(g + c) < rem;
-#pragma unroll
-            for (int k = 0; k < NT; k++)
-                m8[k] |= (ok && is_rec(v, p.keys[k])) ? (1u << c) : 0u;
-        }
-#pragma unroll
-        for (int k = 0; k < NT; k++) mask[k] |= m8[k] << g;
+    for (int k = 0; k < NT; k++) m[k] = 0;
+#pragma unroll 8
+    for (int c = 0; c < 32; c++) {
+        T v = cell_dist_mem<T, NORM, EMB>(xs + c, xsd + c, tau, emb);
+        if (CHECK && (long long)c >= rem) v = never_value<T>();
+        push_cell<NT>(m, v, p.keys);
     }
-#pragma unroll
-    for (int k = 0; k < NT; k++) runs_of_mask(mask[k], carry[k], k, sink);
+    close_block<NT>(m, carry, sink);
 }
 
 template <typename T, int NORM, int EMB, int NT>
@@ -228,7 +229,7 @@ det_diags(const __grid_constant__ WalkArgs p) {
     u32 *sh = smem;
     u32 *shmax = smem + NT * kShortRunBins;
     hist_smem_clear(sh, shmax, NT * kShortRunBins);
-    const HistSink sink{sh, shmax, p.hist, p.hist_stride};
+    const HistSink sink{sh, shmax, p.hist, p.hist_stride, p.row};
 
     const T *__restrict__ x = (const T *)p.x;
     const int lane = threadIdx.x & 31;
@@ -276,27 +277,16 @@ __device__ __forceinline__ void lam_block(const T (&a)[EMB > 0 ? EMB : 1],
                                           long long tau, int emb, long long rem,
                                           const WalkArgs &p, u32 (&carry)[NT],
                                           const HistSink &sink) {
-    u32 mask[NT];
+    u32 m[NT];
 #pragma unroll
-    for (int k = 0; k < NT; k++) mask[k] = 0;
-#pragma unroll 1
-    for (int g = 0; g < 32; g += 8) {
-        u32 m8[NT];
-#pragma unroll
-        for (int k = 0; k < NT; k++) m8[k] = 0;
-#pragma unroll
-        for (int c = 0; c < 8; c++) {
-            T v = cell_dist<T, NORM, EMB>(a, xi, xj + g + c, tau, emb);
-            const bool ok = !CHECK || (long long)(g + c) < rem;
-#pragma unroll
-            for (int k = 0; k < NT; k++)
-                m8[k] |= (ok && is_rec(v, p.keys[k])) ? (1u << c) : 0u;
-        }
-#pragma unroll
-        for (int k = 0; k < NT; k++) mask[k] |= m8[k] << g;
+    for (int k = 0; k < NT; k++) m[k] = 0;
+#pragma unroll 8
+    for (int c = 0; c < 32; c++) {
+        T v = cell_dist<T, NORM, EMB>(a, xi, xj + c, tau, emb);
+        if (CHECK && (long long)c >= rem) v = never_value<T>();
+        push_cell<NT>(m, v, p.keys);
     }
-#pragma unroll
-    for (int k = 0; k < NT; k++) runs_of_mask(mask[k], carry[k], k, sink);
+    close_block<NT>(m, carry, sink);
 }
 
 template <typename T, int NORM, int EMB, int NT>
@@ -306,7 +296,7 @@ lam_rows(const __grid_constant__ WalkArgs p) {
     u32 *sh = smem;
     u32 *shmax = smem + NT * kShortRunBins;
     hist_smem_clear(sh, shmax, NT * kShortRunBins);
-    const HistSink sink{sh, shmax, p.hist, p.hist_stride};
+    const HistSink sink{sh, shmax, p.hist, p.hist_stride, p.row};
 
     const T *__restrict__ x = (const T *)p.x;
     const int lane = threadIdx.x & 31;

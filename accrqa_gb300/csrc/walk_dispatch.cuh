@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <cstring>
 
 #include "engine_abi.h"
 #include "rqa_kernels.cuh"
@@ -44,7 +45,31 @@ static cudaError_t launch_one(const accrqa_walk_desc &d, cudaStream_t st) {
     a.emb = d.emb;
     a.nthr = d.nthr;
     a.pad_ = 0;
-    for (int k = 0; k < kMaxThrPerPass; k++) a.keys[k] = d.keys[k];
+    // Slots in decreasing threshold order (see WalkArgs); the caller's order
+    // is kept in row[].  Padding keys are the never-recurrent minimum.
+    int order[kMaxThrPerPass];
+    for (int k = 0; k < kMaxThrPerPass; k++) order[k] = k;
+    auto wider = [&](int u, int v) {
+        if (u >= d.nthr || v >= d.nthr) return u < v && u < d.nthr;
+        if (d.dtype == ACCRQA_F32) {
+            float fu, fv;
+            const unsigned bu = (unsigned)d.keys[u], bv = (unsigned)d.keys[v];
+            memcpy(&fu, &bu, 4);
+            memcpy(&fv, &bv, 4);
+            return fu > fv;
+        }
+        return d.keys[u] > d.keys[v];
+    };
+    for (int k = 1; k < kMaxThrPerPass; k++)   // insertion sort, stable
+        for (int q = k; q > 0 && wider(order[q], order[q - 1]); q--) {
+            const int t = order[q];
+            order[q] = order[q - 1];
+            order[q - 1] = t;
+        }
+    for (int k = 0; k < kMaxThrPerPass; k++) {
+        a.keys[k] = d.keys[order[k]];
+        a.row[k] = order[k] < d.nthr ? order[k] : 0;
+    }
     a.counts = (u64 *)d.d_counts;
     a.hist = (u64 *)d.d_hist;
     a.hist_stride = d.hist_stride;

@@ -21,7 +21,7 @@ enum accrqa_dtype { ACCRQA_F32 = 0, ACCRQA_F64 = 1 };
 
 #define ACCRQA_MAX_THR_PER_PASS 16
 #define ACCRQA_SERIES_PAD 128
-#define ACCRQA_SHORT_RUN_BINS 512
+#define ACCRQA_SHORT_RUN_BINS 256
 
 /* One kernel pass: one (series, tau, emb, norm) and up to 16 thresholds. */
 typedef struct accrqa_walk_desc {

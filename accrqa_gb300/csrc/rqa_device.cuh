@@ -38,7 +38,7 @@ constexpr int kNormMaximal = 2;
 constexpr int kMaxThrPerPass = 16;
 // Runs shorter than this are binned in shared memory, longer ones go straight
 // to the global histogram.
-constexpr int kShortRunBins = 512;
+constexpr int kShortRunBins = 256;
 
 // Kernel arguments, passed by value so that the threshold keys live in the
 // constant bank and every compare reads its key as an operand.  Slots are
@@ -126,6 +126,39 @@ __device__ __forceinline__ void push_cell(u32 (&m)[NT], double v, const u64 (&ke
     const u64 b = (u64)__double_as_longlong(v);
 #pragma unroll
     for (int k = 0; k < NT; k++) m[k] = (m[k] << 1) | (b >= keys[k] ? 1u : 0u);
+}
+
+// Cells are pushed in groups of kGroup.  When no cell of a group passes the
+// widest threshold (slot 0), every mask just takes kGroup "not recurrent"
+// bits -- one operation per slot instead of two per slot and cell.
+constexpr int kGroup = 8;
+
+__device__ __forceinline__ bool group_any(const float (&v)[kGroup], u64 key0) {
+    float lo = v[0];
+#pragma unroll
+    for (int g = 1; g < kGroup; g++) lo = fminf(lo, v[g]);   // NaN-ignoring
+    return is_rec(lo, key0);
+}
+__device__ __forceinline__ bool group_any(const double (&v)[kGroup], u64 key0) {
+    u64 lo = (u64)__double_as_longlong(v[0]);
+#pragma unroll
+    for (int g = 1; g < kGroup; g++) {
+        const u64 b = (u64)__double_as_longlong(v[g]);
+        lo = b < lo ? b : lo;
+    }
+    return lo < key0;
+}
+
+template <typename T, int NT>
+__device__ __forceinline__ void push_group(u32 (&m)[NT], const T (&v)[kGroup],
+                                           const u64 (&keys)[kMaxThrPerPass]) {
+    if (!group_any(v, keys[0])) {
+#pragma unroll
+        for (int k = 0; k < NT; k++) m[k] = (m[k] << kGroup) | ((1u << kGroup) - 1u);
+    } else {
+#pragma unroll
+        for (int g = 0; g < kGroup; g++) push_cell<NT>(m, v[g], keys);
+    }
 }
 
 // Value that is never recurrent (for cells past the end of a line).

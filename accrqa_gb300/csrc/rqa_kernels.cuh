@@ -105,21 +105,89 @@ __device__ __forceinline__ void hist_smem_flush(const u32 *sh, const u32 *shmax,
         if (shmax[t]) atomicMax(&p.maxlen[p.row[t]], shmax[t]);
 }
 
-// Close the runs of one 32-cell block for every slot.  Slots nest (slot 0 is
-// the widest threshold), so when slot 0 has neither a recurrent cell nor an
-// open run, no slot has one and the block needs no work.
+// Per-warp run state in shared memory: the 32 lanes' masks and open-run
+// lengths of every slot, [slot][lane].  Keeping them out of registers lets the
+// slot loop below stay a loop (small code, no instruction-cache misses) and
+// stop at the first empty slot.
+struct LaneRuns {
+    u32 *mask;    // [NT][32]
+    u32 *carry;   // [NT][32]
+    int lane;
+    __device__ __forceinline__ u32 &m(int k) const { return mask[k * 32 + lane]; }
+    __device__ __forceinline__ u32 &c(int k) const { return carry[k * 32 + lane]; }
+};
+
 template <int NT>
-__device__ __forceinline__ void close_block(const u32 (&m)[NT], u32 (&carry)[NT],
-                                            const HistSink &sink) {
-    if ((walk_mask(m[0]) | carry[0]) == 0u) return;
-#pragma unroll
-    for (int k = 0; k < NT; k++) runs_of_mask(walk_mask(m[k]), carry[k], k, sink);
+__device__ __forceinline__ void runs_begin(const LaneRuns &r) {
+#pragma unroll 1
+    for (int k = 0; k < NT; k++) r.c(k) = 0;
 }
+
+// Close the runs of one 32-cell block for every slot.  Slots nest (slot 0 is
+// the widest threshold): when slot 0 has neither a recurrent cell nor an open
+// run, no slot has one; otherwise slots are visited until the first empty one.
+template <int NT>
+__device__ __forceinline__ void close_block(const u32 (&m)[NT], const LaneRuns &r,
+                                            const HistSink &sink) {
+    if ((walk_mask(m[0]) | r.c(0)) == 0u) return;
+#pragma unroll
+    for (int k = 0; k < NT; k++) r.m(k) = m[k];
+#pragma unroll 1
+    for (int k = 0; k < NT; k++) {
+        const u32 rec = walk_mask(r.m(k));
+        u32 carry = r.c(k);
+        if ((rec | carry) == 0u) break;
+        runs_of_mask(rec, carry, k, sink);
+        r.c(k) = carry;
+    }
+}
+
+// End of a line: every open run is complete.
+template <int NT>
+__device__ __forceinline__ void runs_end(const LaneRuns &r, const HistSink &sink) {
+#pragma unroll 1
+    for (int k = 0; k < NT; k++) {
+        const u32 carry = r.c(k);
+        if (carry == 0u) break;   // nested: later slots have shorter runs
+        sink.emit(k, carry);
+        r.c(k) = 0;
+    }
+}
+
+// Shared memory of the line kernels: histogram bins, longest-run markers and
+// the per-warp run state.
+template <int NT>
+struct LineSmem {
+    static constexpr int kWords = NT * kShortRunBins + kMaxThrPerPass + 2 * kWarpsPerCta * NT * 32;
+    static constexpr size_t kBytes = (size_t)kWords * sizeof(u32);
+};
 
 // ---------------------------------------------------------------------------
 // RR: lane r of a warp owns row i = 32*band + r and walks the columns j >= i;
 // the main-diagonal cell (i, i) is counted once, the others twice.
 // ---------------------------------------------------------------------------
+template <typename T, int NORM, int EMB, int NT, bool CHECK>
+__device__ __forceinline__ void rr_block(const T (&a)[EMB > 0 ? EMB : 1],
+                                         const T *__restrict__ xi, const T *__restrict__ xj,
+                                         long long tau, int emb, long long lo, long long hi,
+                                         const WalkArgs &p, u32 (&up)[NT]) {
+    u32 m[NT];
+#pragma unroll
+    for (int k = 0; k < NT; k++) m[k] = 0;
+#pragma unroll 1
+    for (int g = 0; g < 32; g += kGroup) {
+        T v[kGroup];
+#pragma unroll
+        for (int c = 0; c < kGroup; c++) {
+            v[c] = cell_dist<T, NORM, EMB>(a, xi, xj + g + c, tau, emb);
+            if (CHECK && !(g + c >= lo && g + c < hi)) v[c] = never_value<T>();
+        }
+        push_group<T, NT>(m, v, p.keys);
+    }
+#pragma unroll
+    for (int k = 0; k < NT; k++) up[k] += 32u - __popc(m[k]);
+}
+
 template <typename T, int NORM, int EMB, int NT>
 __global__ void __launch_bounds__(kWarpsPerCta * 32)
 rr_rows(const __grid_constant__ WalkArgs p) {
@@ -143,49 +211,25 @@ rr_rows(const __grid_constant__ WalkArgs p) {
             const bool row_ok = i < nc;
             T a[EMB > 0 ? EMB : 1];
             load_lane_vec<T, EMB>(a, x + i, tau);
-            u32 up[NT], dg[NT], m[NT];
+            u32 up[NT], dg[NT];
             {
                 const T v = cell_dist<T, NORM, EMB>(a, x + i, x + i, tau, p.emb);
 #pragma unroll
                 for (int k = 0; k < NT; k++) {
                     dg[k] = (row_ok && is_rec(v, p.keys[k])) ? 1u : 0u;
                     up[k] = 0;
-                    m[k] = 0;
                 }
             }
-            // first block: the columns j > i of the diagonal tile
+            // first block: the columns j > i of the diagonal tile (j < nc)
             const long long j0 = band * 32;
-#pragma unroll 4
-            for (int c = 0; c < 32; c++) {
-                const long long j = j0 + c;
-                T v = cell_dist<T, NORM, EMB>(a, x + i, x + j, tau, p.emb);
-                if (!(j > i && j < nc)) v = never_value<T>();
-                push_cell<NT>(m, v, p.keys);
-            }
-#pragma unroll
-            for (int k = 0; k < NT; k++) up[k] += 32u - __popc(m[k]);
+            long long hi0 = nc - j0 < 32 ? nc - j0 : 32;
+            rr_block<T, NORM, EMB, NT, true>(a, x + i, x + j0, tau, p.emb, lane + 1, hi0, p, up);
             // full blocks: j > i for every lane, all columns inside the matrix
             long long jb = j0 + 32;
-            for (; jb + 32 <= nc; jb += 32) {
-                const T *xj = x + jb;
-#pragma unroll 8
-                for (int c = 0; c < 32; c++)
-                    push_cell<NT>(m, cell_dist<T, NORM, EMB>(a, x + i, xj + c, tau, p.emb), p.keys);
-#pragma unroll
-                for (int k = 0; k < NT; k++) up[k] += 32u - __popc(m[k]);
-            }
-            // tail block
-            if (jb < nc) {
-#pragma unroll 4
-                for (int c = 0; c < 32; c++) {
-                    const long long j = jb + c;
-                    T v = cell_dist<T, NORM, EMB>(a, x + i, x + j, tau, p.emb);
-                    if (j >= nc) v = never_value<T>();
-                    push_cell<NT>(m, v, p.keys);
-                }
-#pragma unroll
-                for (int k = 0; k < NT; k++) up[k] += 32u - __popc(m[k]);
-            }
+            for (; jb + 32 <= nc; jb += 32)
+                rr_block<T, NORM, EMB, NT, false>(a, x + i, x + jb, tau, p.emb, 0, 32, p, up);
+            if (jb < nc)
+                rr_block<T, NORM, EMB, NT, true>(a, x + i, x + jb, tau, p.emb, 0, nc - jb, p, up);
 #pragma unroll
             for (int k = 0; k < NT; k++) {
                 u64 t = 2ull * (u64)(row_ok ? up[k] : 0u) + (u64)dg[k];
@@ -208,18 +252,22 @@ template <typename T, int NORM, int EMB, int NT, bool CHECK>
 __device__ __forceinline__ void det_block(const T *__restrict__ xs,
                                           const T *__restrict__ xsd,
                                           long long tau, int emb, long long rem,
-                                          const WalkArgs &p, u32 (&carry)[NT],
+                                          const WalkArgs &p, const LaneRuns &r,
                                           const HistSink &sink) {
     u32 m[NT];
 #pragma unroll
     for (int k = 0; k < NT; k++) m[k] = 0;
-#pragma unroll 8
-    for (int c = 0; c < 32; c++) {
-        T v = cell_dist_mem<T, NORM, EMB>(xs + c, xsd + c, tau, emb);
-        if (CHECK && (long long)c >= rem) v = never_value<T>();
-        push_cell<NT>(m, v, p.keys);
+#pragma unroll 1
+    for (int g = 0; g < 32; g += kGroup) {
+        T v[kGroup];
+#pragma unroll
+        for (int c = 0; c < kGroup; c++) {
+            v[c] = cell_dist_mem<T, NORM, EMB>(xs + g + c, xsd + g + c, tau, emb);
+            if (CHECK && (long long)(g + c) >= rem) v[c] = never_value<T>();
+        }
+        push_group<T, NT>(m, v, p.keys);
     }
-    close_block<NT>(m, carry, sink);
+    close_block<NT>(m, r, sink);
 }
 
 template <typename T, int NORM, int EMB, int NT>
@@ -228,12 +276,14 @@ det_diags(const __grid_constant__ WalkArgs p) {
     extern __shared__ u32 smem[];
     u32 *sh = smem;
     u32 *shmax = smem + NT * kShortRunBins;
+    u32 *runs = shmax + kMaxThrPerPass;
     hist_smem_clear(sh, shmax, NT * kShortRunBins);
     const HistSink sink{sh, shmax, p.hist, p.hist_stride, p.row};
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const LaneRuns r{runs + warp * 2 * NT * 32, runs + warp * 2 * NT * 32 + NT * 32, lane};
 
     const T *__restrict__ x = (const T *)p.x;
-    const int lane = threadIdx.x & 31;
-    const long long gwarp = (long long)blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);
+    const long long gwarp = (long long)blockIdx.x * kWarpsPerCta + warp;
     const long long nwarps = (long long)gridDim.x * kWarpsPerCta;
     const long long nc = p.nc;
     const long long tau = p.tau;
@@ -247,19 +297,15 @@ det_diags(const __grid_constant__ WalkArgs p) {
             const long long len = nc - d;                 // cells on this diagonal
             const long long wmin = nc - (band * 32 + 32); // shortest diagonal of the warp
             const long long wmax = nc - (band * 32 + 1);  // longest diagonal of the warp
-            u32 carry[NT];
-#pragma unroll
-            for (int k = 0; k < NT; k++) carry[k] = 0;
+            runs_begin<NT>(r);
             long long s0 = 0;
             for (; s0 + 32 <= wmin; s0 += 32)
-                det_block<T, NORM, EMB, NT, false>(x + s0, x + s0 + d, tau, p.emb,
-                                                   32, p, carry, sink);
+                det_block<T, NORM, EMB, NT, false>(x + s0, x + s0 + d, tau, p.emb, 32, p, r,
+                                                   sink);
             for (; s0 < wmax; s0 += 32)
-                det_block<T, NORM, EMB, NT, true>(x + s0, x + s0 + d, tau, p.emb,
-                                                  len - s0, p, carry, sink);
-#pragma unroll
-            for (int k = 0; k < NT; k++)
-                if (carry[k]) sink.emit(k, carry[k]);
+                det_block<T, NORM, EMB, NT, true>(x + s0, x + s0 + d, tau, p.emb, len - s0,
+                                                  p, r, sink);
+            runs_end<NT>(r, sink);
         }
     }
     hist_smem_flush(sh, shmax, p);
@@ -275,18 +321,22 @@ __device__ __forceinline__ void lam_block(const T (&a)[EMB > 0 ? EMB : 1],
                                           const T *__restrict__ xi,
                                           const T *__restrict__ xj,
                                           long long tau, int emb, long long rem,
-                                          const WalkArgs &p, u32 (&carry)[NT],
+                                          const WalkArgs &p, const LaneRuns &r,
                                           const HistSink &sink) {
     u32 m[NT];
 #pragma unroll
     for (int k = 0; k < NT; k++) m[k] = 0;
-#pragma unroll 8
-    for (int c = 0; c < 32; c++) {
-        T v = cell_dist<T, NORM, EMB>(a, xi, xj + c, tau, emb);
-        if (CHECK && (long long)c >= rem) v = never_value<T>();
-        push_cell<NT>(m, v, p.keys);
+#pragma unroll 1
+    for (int g = 0; g < 32; g += kGroup) {
+        T v[kGroup];
+#pragma unroll
+        for (int c = 0; c < kGroup; c++) {
+            v[c] = cell_dist<T, NORM, EMB>(a, xi, xj + g + c, tau, emb);
+            if (CHECK && (long long)(g + c) >= rem) v[c] = never_value<T>();
+        }
+        push_group<T, NT>(m, v, p.keys);
     }
-    close_block<NT>(m, carry, sink);
+    close_block<NT>(m, r, sink);
 }
 
 template <typename T, int NORM, int EMB, int NT>
@@ -295,12 +345,14 @@ lam_rows(const __grid_constant__ WalkArgs p) {
     extern __shared__ u32 smem[];
     u32 *sh = smem;
     u32 *shmax = smem + NT * kShortRunBins;
+    u32 *runs = shmax + kMaxThrPerPass;
     hist_smem_clear(sh, shmax, NT * kShortRunBins);
     const HistSink sink{sh, shmax, p.hist, p.hist_stride, p.row};
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const LaneRuns r{runs + warp * 2 * NT * 32, runs + warp * 2 * NT * 32 + NT * 32, lane};
 
     const T *__restrict__ x = (const T *)p.x;
-    const int lane = threadIdx.x & 31;
-    const long long gwarp = (long long)blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);
+    const long long gwarp = (long long)blockIdx.x * kWarpsPerCta + warp;
     const long long nwarps = (long long)gridDim.x * kWarpsPerCta;
     const long long nc = p.nc;
     const long long tau = p.tau;
@@ -310,20 +362,15 @@ lam_rows(const __grid_constant__ WalkArgs p) {
         const bool row_ok = i < nc;
         T a[EMB > 0 ? EMB : 1];
         load_lane_vec<T, EMB>(a, x + i, tau);
-        u32 carry[NT];
-#pragma unroll
-        for (int k = 0; k < NT; k++) carry[k] = 0;
+        runs_begin<NT>(r);
         long long j0 = 0;
         if (row_ok) {
             for (; j0 + 32 <= nc; j0 += 32)
-                lam_block<T, NORM, EMB, NT, false>(a, x + i, x + j0, tau, p.emb, 32, p,
-                                                   carry, sink);
+                lam_block<T, NORM, EMB, NT, false>(a, x + i, x + j0, tau, p.emb, 32, p, r, sink);
             if (j0 < nc)
-                lam_block<T, NORM, EMB, NT, true>(a, x + i, x + j0, tau, p.emb, nc - j0,
-                                                  p, carry, sink);
-#pragma unroll
-            for (int k = 0; k < NT; k++)
-                if (carry[k]) sink.emit(k, carry[k]);
+                lam_block<T, NORM, EMB, NT, true>(a, x + i, x + j0, tau, p.emb, nc - j0, p, r,
+                                                  sink);
+            runs_end<NT>(r, sink);
         }
     }
     hist_smem_flush(sh, shmax, p);

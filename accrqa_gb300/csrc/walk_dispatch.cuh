@@ -24,10 +24,10 @@ static cudaError_t launch_one(const accrqa_walk_desc &d, cudaStream_t st) {
         kern = rr_rows<T, NORM, EMB, NT>;
     } else if (KIND == ACCRQA_WALK_DET) {
         kern = det_diags<T, NORM, EMB, NT>;
-        smem = (size_t)(NT * kShortRunBins + kMaxThrPerPass) * sizeof(u32);
+        smem = LineSmem<NT>::kBytes;
     } else {
         kern = lam_rows<T, NORM, EMB, NT>;
-        smem = (size_t)(NT * kShortRunBins + kMaxThrPerPass) * sizeof(u32);
+        smem = LineSmem<NT>::kBytes;
     }
     // Resident CTAs per SM for this instantiation, computed once.
     static int per_sm = -1;

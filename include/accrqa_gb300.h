@@ -251,7 +251,7 @@ Accrqa_Error accrqa_gb300_measures(double *out5, const uint64_t *hist,
  * the caller.  Thresholds are host values of the series dtype.
  *   rr : d_counts[k] += full-matrix recurrent cells
  *   det: d_hist[k*stride + l] += strict-upper-triangle diagonal runs
- *        (not doubled, no line of identity), d_maxlen[k] = longest run >= 512
+ *        (not doubled, no line of identity), d_maxlen[k] = longest run >= 256
  *   lam: d_hist[k*stride + l] += row runs of the full matrix
  * nthr may exceed 16; passes of 16 are enqueued back to back. */
 Accrqa_Error accrqa_gb300_rr_counts_dev(uint64_t *d_counts, const void *d_x,

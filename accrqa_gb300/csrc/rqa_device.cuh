@@ -149,10 +149,14 @@ __device__ __forceinline__ bool group_any(const double (&v)[kGroup], u64 key0) {
     return lo < key0;
 }
 
+// The decision is taken for the whole warp (all lanes call this together): a
+// lane with nothing recurrent in a group that another lane needs simply pushes
+// its all-"not recurrent" bits through the per-cell path, which keeps the
+// warp on one path instead of serialising both.
 template <typename T, int NT>
 __device__ __forceinline__ void push_group(u32 (&m)[NT], const T (&v)[kGroup],
                                            const u64 (&keys)[kMaxThrPerPass]) {
-    if (!group_any(v, keys[0])) {
+    if (!__any_sync(0xFFFFFFFFu, group_any(v, keys[0]))) {
 #pragma unroll
         for (int k = 0; k < NT; k++) m[k] = (m[k] << kGroup) | ((1u << kGroup) - 1u);
     } else {

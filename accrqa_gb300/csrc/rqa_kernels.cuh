@@ -364,14 +364,20 @@ lam_rows(const __grid_constant__ WalkArgs p) {
         load_lane_vec<T, EMB>(a, x + i, tau);
         runs_begin<NT>(r);
         long long j0 = 0;
-        if (row_ok) {
+        // All lanes walk together (the group decision is warp-wide); in the
+        // last, partial band the rows past nc see only never-recurrent cells.
+        if (band * 32 + 31 < nc) {
             for (; j0 + 32 <= nc; j0 += 32)
                 lam_block<T, NORM, EMB, NT, false>(a, x + i, x + j0, tau, p.emb, 32, p, r, sink);
             if (j0 < nc)
                 lam_block<T, NORM, EMB, NT, true>(a, x + i, x + j0, tau, p.emb, nc - j0, p, r,
                                                   sink);
-            runs_end<NT>(r, sink);
+        } else {
+            for (; j0 < nc; j0 += 32)
+                lam_block<T, NORM, EMB, NT, true>(a, x + i, x + j0, tau, p.emb,
+                                                  row_ok ? nc - j0 : 0, p, r, sink);
         }
+        runs_end<NT>(r, sink);
     }
     hist_smem_flush(sh, shmax, p);
 }

@@ -208,6 +208,10 @@ void accrqa_gb300_transfer_stats(uint64_t *h2d_bytes, uint64_t *d2h_bytes, int32
 
 uint64_t accrqa_gb300_kernel_launches(void) { return accrqa_gb300_launch_count(); }
 
+Accrqa_Error accrqa_gb300_batch(const accrqa_gb300_series_job *jobs, int32_t njobs) {
+    return run_batch(jobs, njobs);
+}
+
 int accrqa_gb300_device_count(void) {
     int n = 0;
     if (cudaGetDeviceCount(&n) != cudaSuccess) {

@@ -84,6 +84,11 @@ static cudaError_t copy2d_d2h_async(void *dst, size_t dpitch, const void *src, s
                              st);
 }
 
+void transfer_stats_add(size_t h2d, size_t d2h) {
+    g_h2d.fetch_add(h2d);
+    g_d2h.fetch_add(d2h);
+}
+
 void transfer_stats(uint64_t *h2d, uint64_t *d2h, int reset) {
     if (h2d) *h2d = g_h2d.load();
     if (d2h) *d2h = g_d2h.load();

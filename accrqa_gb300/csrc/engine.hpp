@@ -26,6 +26,7 @@ Accrqa_Error cuda_error(cudaError_t e, const char *what);
 // Bytes copied host->device and device->host by the engine since load (or
 // since the last reset).
 void transfer_stats(uint64_t *h2d, uint64_t *d2h, int reset);
+void transfer_stats_add(size_t h2d, size_t d2h);
 
 // ---- device memory --------------------------------------------------------
 // Grow-only device allocation owned by a context.
@@ -44,7 +45,18 @@ struct Context {
     std::mutex mu;
     DeviceBuffer series, counts, hist, maxlen, rp[2];
     std::vector<uint64_t> host_u64;
+    // batched path: side streams for concurrent launch groups, a device arena
+    // for descriptors and results, and pinned staging for one-copy uploads
+    std::vector<cudaStream_t> side;
+    DeviceBuffer arena;
+    void *pinned = nullptr;
+    size_t pinned_bytes = 0;
 };
+
+// Grow-only pinned host staging of a context (cudaHostAlloc).
+cudaError_t pinned_reserve(Context &c, size_t bytes);
+// At least n side streams of a context.
+cudaError_t side_streams(Context &c, int n);
 
 // Context of the calling thread's current device, created on first use.
 // Returns nullptr and sets *err when no usable device exists.
@@ -109,6 +121,9 @@ Accrqa_Error run_lines(int kind, T *out, const T *x, size_t n, const int *taus,
 template <typename T, typename OUT>
 Accrqa_Error run_rp(OUT *out, const T *x, size_t n, int tau, int emb, T thr,
                     int norm);
+
+// Many series in one submission (accrqa_gb300_batch).
+Accrqa_Error run_batch(const accrqa_gb300_series_job *jobs, int njobs);
 
 // Raw results for the engine C ABI (full-convention histograms).
 template <typename T>

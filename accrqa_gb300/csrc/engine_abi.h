@@ -22,6 +22,7 @@ enum accrqa_dtype { ACCRQA_F32 = 0, ACCRQA_F64 = 1 };
 #define ACCRQA_MAX_THR_PER_PASS 16
 #define ACCRQA_SERIES_PAD 128
 #define ACCRQA_SHORT_RUN_BINS 256
+#define ACCRQA_BATCH_BINS 128   /* short-run bins of the batched kernels */
 
 /* One kernel pass: one (series, tau, emb, norm) and up to 16 thresholds. */
 typedef struct accrqa_walk_desc {
@@ -56,6 +57,51 @@ int accrqa_gb300_sm_count(void);
 
 /* Kernels this library has launched since it was loaded. */
 uint64_t accrqa_gb300_launch_count(void);
+
+/* ---- batched passes (many series per launch) ---------------------------- */
+
+/* One series' pass as the batched kernels read it (device memory).  Keys are
+ * sorted by decreasing threshold, row[k] is the output row of slot k, padding
+ * slots hold the never-recurrent key.  Same layout as accrqa::BatchJob. */
+typedef struct accrqa_batch_job {
+    const void *x;
+    int64_t nc;
+    int64_t nbands;
+    int32_t tau;
+    int32_t emb;
+    int32_t nthr;
+    int32_t pad_;
+    uint64_t keys[ACCRQA_MAX_THR_PER_PASS];
+    int32_t row[ACCRQA_MAX_THR_PER_PASS];
+    uint64_t *counts;
+    uint64_t *hist;
+    int64_t hist_stride;
+    uint32_t *maxlen;
+} accrqa_batch_job;
+
+typedef struct accrqa_batch_unit {
+    int32_t job;
+    int32_t unit;
+} accrqa_batch_unit;
+
+/* One batched launch: every job of one kernel shape. */
+typedef struct accrqa_batch_launch {
+    int32_t kind;            /* accrqa_walk_kind */
+    int32_t dtype;
+    int32_t norm;
+    int32_t emb;             /* the jobs' emb (they share it) */
+    int32_t nt;              /* threshold slots: 8 or 16 */
+    int32_t nwarps;          /* warps in the launch (== ranges in d_warp_begin) */
+    const void *d_jobs;      /* accrqa_batch_job[] */
+    const void *d_units;     /* accrqa_batch_unit[], ordered by job */
+    const int32_t *d_warp_begin; /* [nwarps + 1] unit range of each warp */
+} accrqa_batch_launch;
+
+/* Enqueue a batched launch.  Returns 0 or a cudaError_t value. */
+int accrqa_gb300_launch_batch(const accrqa_batch_launch *L, void *stream);
+
+/* Resident warps of the batched kernel for this shape (sizes the ranges). */
+int accrqa_gb300_batch_warps(const accrqa_batch_launch *L);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,446 @@
+// engine_batch.cpp -- many series in one submission (accrqa_gb300_batch).
+//
+// Every series of a batch brings its own length, tau, emb, norm and
+// thresholds.  The batch is planned on the host:
+//   1. all series go into one device arena with one host-to-device copy from
+//      pinned staging;
+//   2. each (series, measure, 16-threshold chunk) becomes a pass descriptor;
+//      passes are grouped by kernel shape (measure, dtype, norm, emb, slots);
+//   3. each group's work units (bands or band pairs of all its series) are
+//      split into one contiguous range per resident warp with equal cells;
+//   4. the groups run concurrently on side streams, captured into one CUDA
+//      graph and launched once;
+//   5. counts and the non-zero histogram prefixes come back in one pass and
+//      are post-processed exactly as the single-series API does, so every
+//      result equals what the plain calls return.
+#include <cuda_runtime_api.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <tuple>
+#include <vector>
+
+#include "engine.hpp"
+
+namespace accrqa {
+
+#define CUB(call, what)                                     \
+    do {                                                    \
+        cudaError_t e_ = (call);                            \
+        if (e_ != cudaSuccess) return cuda_error(e_, what); \
+    } while (0)
+
+cudaError_t pinned_reserve(Context &c, size_t bytes) {
+    if (bytes <= c.pinned_bytes && c.pinned) return cudaSuccess;
+    if (c.pinned) cudaFreeHost(c.pinned);
+    c.pinned = nullptr;
+    c.pinned_bytes = 0;
+    const size_t grow = bytes + bytes / 4 + 4096;
+    cudaError_t e = cudaHostAlloc(&c.pinned, grow, cudaHostAllocDefault);
+    if (e != cudaSuccess) {
+        c.pinned = nullptr;
+        return e;
+    }
+    c.pinned_bytes = grow;
+    return cudaSuccess;
+}
+
+cudaError_t side_streams(Context &c, int n) {
+    while ((int)c.side.size() < n) {
+        cudaStream_t s;
+        cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+        if (e != cudaSuccess) return e;
+        c.side.push_back(s);
+    }
+    return cudaSuccess;
+}
+
+namespace {
+
+constexpr int kSideStreams = 4;
+
+size_t align16(size_t v) { return (v + 15) & ~(size_t)15; }
+
+struct Pass {
+    int job;
+    int kind;
+    int k0, cnt;
+    int64_t nc;
+    size_t counts_off = 0, maxlen_off = 0, hist_off = 0;   // arena byte offsets
+    accrqa_batch_job desc;
+};
+
+// (kind, dtype, norm, emb key, slots)
+typedef std::tuple<int, int, int, int, int> GroupKey;
+
+int emb_key(int dtype, int emb) {
+    return (dtype == ACCRQA_F32 && emb >= 2 && emb <= 8) ? emb : 0;
+}
+
+template <typename T>
+uint64_t key_of(const void *thr, int k, int norm) {
+    return threshold_key<T>(((const T *)thr)[k], norm);
+}
+
+Accrqa_Error check_job(const accrqa_gb300_series_job &j) {
+    if (!j.x || !j.thresholds) return ERR_MEM_ALLOC_FAILURE;
+    if (j.dtype != ACCRQA_GB300_F32 && j.dtype != ACCRQA_GB300_F64) return ERR_DATA_TYPE;
+    if (j.n < 1 || j.tau < 1 || j.emb < 1 || j.nthr < 1 ||
+        j.n - (int64_t)(j.emb - 1) * j.tau < 1 || j.n > ((int64_t)1 << 31) ||
+        (j.norm != DST_EUCLIDEAN && j.norm != DST_MAXIMAL) || j.lmin < 0 || j.vmin < 0) {
+        set_last_error("invalid series job");
+        return ERR_INVALID_ARGUMENT;
+    }
+    return SUCCESS;
+}
+
+template <typename T>
+void write_line_out(void *out, int k, const LineHistogram &h, int lmin, bool full, bool is_det) {
+    T *o = (T *)out + 5 * (size_t)k;
+    const int64_t nc = h.nc();
+    o[0] = (T)h.primary(lmin);
+    o[1] = (T)h.secondary(lmin);
+    o[2] = (T)(full ? h.tertiary(is_det ? 1 : 0) : NAN);
+    o[3] = (T)(full ? h.quaternary(lmin) : NAN);
+    if (full) {
+        o[4] = (T)h.rr();
+    } else {
+        const uint64_t d1 = (uint64_t)nc - 1;
+        o[4] = (T)((double)h.metric(0) / (double)(d1 * d1));
+    }
+}
+
+}  // namespace
+
+// One sub-batch whose device memory fits; jobs [j0, j1).
+static Accrqa_Error run_batch_part(Context &c, const accrqa_gb300_series_job *jobs, int j0,
+                                   int j1) {
+    // ---- plan -------------------------------------------------------------
+    std::vector<size_t> xoff((size_t)(j1 - j0));
+    size_t series_bytes = 0;
+    for (int j = j0; j < j1; j++) {
+        const size_t es = jobs[j].dtype == ACCRQA_GB300_F32 ? 4 : 8;
+        xoff[(size_t)(j - j0)] = series_bytes;
+        series_bytes = align16(series_bytes + (size_t)(jobs[j].n + ACCRQA_SERIES_PAD) * es);
+    }
+    std::vector<Pass> passes;
+    for (int j = j0; j < j1; j++) {
+        const accrqa_gb300_series_job &J = jobs[j];
+        const int kinds[3] = {ACCRQA_WALK_RR, ACCRQA_WALK_DET, ACCRQA_WALK_LAM};
+        void *outs[3] = {J.rr_out, J.det_out, J.lam_out};
+        for (int q = 0; q < 3; q++) {
+            if (!outs[q]) continue;
+            for (int k0 = 0; k0 < J.nthr; k0 += ACCRQA_MAX_THR_PER_PASS) {
+                Pass p;
+                p.job = j;
+                p.kind = kinds[q];
+                p.k0 = k0;
+                p.cnt = std::min(J.nthr - k0, ACCRQA_MAX_THR_PER_PASS);
+                p.nc = J.n - (int64_t)(J.emb - 1) * J.tau;
+                passes.push_back(p);
+            }
+        }
+    }
+    // arena layout: series | counts | maxlen | histograms | job tables | units | ranges
+    size_t off = series_bytes;
+    for (Pass &p : passes) {
+        if (p.kind == ACCRQA_WALK_RR) {
+            p.counts_off = off;
+            off += 16 * 8;
+        }
+    }
+    for (Pass &p : passes) {
+        if (p.kind != ACCRQA_WALK_RR) {
+            p.maxlen_off = off;
+            off += 16 * 4;
+        }
+    }
+    const size_t head_end = off;   // counts and longest-run markers end here
+    off = align16(off);
+    const size_t zero_begin = series_bytes;
+    for (Pass &p : passes) {
+        if (p.kind != ACCRQA_WALK_RR) {
+            p.hist_off = off;
+            off += (size_t)p.cnt * (size_t)(p.nc + 1) * 8;
+        }
+    }
+    const size_t zero_end = off;
+
+    std::map<GroupKey, std::vector<int>> groups;
+    for (int i = 0; i < (int)passes.size(); i++) {
+        const Pass &p = passes[(size_t)i];
+        const accrqa_gb300_series_job &J = jobs[p.job];
+        const int nt = p.cnt <= 8 ? 8 : 16;
+        groups[GroupKey(p.kind, J.dtype, J.norm, emb_key(J.dtype, J.emb), nt)].push_back(i);
+    }
+    struct GroupPlan {
+        accrqa_batch_launch L;
+        size_t jobs_off, units_off, ranges_off;
+        std::vector<accrqa_batch_job> table;
+        std::vector<accrqa_batch_unit> units;
+        std::vector<int32_t> ranges;
+    };
+    std::vector<GroupPlan> plans;
+    for (auto &g : groups) {
+        GroupPlan gp;
+        std::memset(&gp.L, 0, sizeof(gp.L));
+        gp.L.kind = std::get<0>(g.first);
+        gp.L.dtype = std::get<1>(g.first);
+        gp.L.norm = std::get<2>(g.first);
+        gp.L.emb = std::get<3>(g.first);
+        gp.L.nt = std::get<4>(g.first);
+        std::vector<int64_t> cost;
+        for (int pi : g.second) {
+            Pass &p = passes[(size_t)pi];
+            const accrqa_gb300_series_job &J = jobs[p.job];
+            accrqa_batch_job d;
+            std::memset(&d, 0, sizeof(d));
+            d.nc = p.nc;
+            d.tau = J.tau;
+            d.emb = J.emb;
+            d.nthr = p.cnt;
+            // keys sorted by decreasing threshold; padding never recurrent
+            uint64_t raw[ACCRQA_MAX_THR_PER_PASS];
+            int order[ACCRQA_MAX_THR_PER_PASS];
+            for (int k = 0; k < p.cnt; k++) {
+                raw[k] = J.dtype == ACCRQA_GB300_F32 ? key_of<float>(J.thresholds, p.k0 + k, J.norm)
+                                                     : key_of<double>(J.thresholds, p.k0 + k, J.norm);
+                order[k] = k;
+            }
+            auto wider = [&](int u, int v) {
+                if (J.dtype == ACCRQA_GB300_F32) {
+                    float fu, fv;
+                    const uint32_t bu = (uint32_t)raw[u], bv = (uint32_t)raw[v];
+                    std::memcpy(&fu, &bu, 4);
+                    std::memcpy(&fv, &bv, 4);
+                    return fu > fv;
+                }
+                return raw[u] > raw[v];
+            };
+            std::stable_sort(order, order + p.cnt, wider);
+            const uint64_t never = J.dtype == ACCRQA_GB300_F32 ? 0xBF800000ull : 0ull;
+            for (int k = 0; k < ACCRQA_MAX_THR_PER_PASS; k++) {
+                d.keys[k] = k < p.cnt ? raw[order[k]] : never;
+                d.row[k] = k < p.cnt ? order[k] : 0;
+            }
+            d.hist_stride = p.nc + 1;
+            const int64_t nbands = p.kind == ACCRQA_WALK_DET ? (p.nc - 1 + 31) / 32 : (p.nc + 31) / 32;
+            d.nbands = nbands;
+            const int64_t nunits = p.kind == ACCRQA_WALK_LAM ? nbands : (nbands + 1) / 2;
+            const int ji = (int)gp.table.size();
+            gp.table.push_back(d);
+            for (int64_t u = 0; u < nunits; u++) {
+                gp.units.push_back(accrqa_batch_unit{ji, (int32_t)u});
+                cost.push_back(p.nc + 64);   // cells per lane, plus a per-unit overhead
+            }
+        }
+        const int resident = accrqa_gb300_batch_warps(&gp.L);
+        if (resident <= 0) {
+            set_last_error("batched kernel unavailable for this shape");
+            return ERR_CUDA;
+        }
+        const int nw = (int)std::min<int64_t>((int64_t)resident, (int64_t)gp.units.size());
+        int64_t total = 0;
+        for (int64_t v : cost) total += v;
+        gp.ranges.assign((size_t)nw + 1, (int32_t)gp.units.size());
+        gp.ranges[0] = 0;
+        int64_t acc = 0;
+        int w = 1;
+        for (size_t u = 0; u < gp.units.size() && w < nw; u++) {
+            acc += cost[u];
+            while (w < nw && acc * nw >= total * w) gp.ranges[(size_t)w++] = (int32_t)(u + 1);
+        }
+        gp.L.nwarps = nw;
+        gp.jobs_off = align16(off);
+        off = gp.jobs_off + gp.table.size() * sizeof(accrqa_batch_job);
+        gp.units_off = align16(off);
+        off = gp.units_off + gp.units.size() * sizeof(accrqa_batch_unit);
+        gp.ranges_off = align16(off);
+        off = gp.ranges_off + gp.ranges.size() * sizeof(int32_t);
+        // pointer fields are filled once the arena address is known
+        for (int pi_i = 0; pi_i < (int)g.second.size(); pi_i++) gp.table[(size_t)pi_i].pad_ = g.second[(size_t)pi_i];
+        plans.push_back(std::move(gp));
+    }
+    const size_t arena_bytes = align16(off);
+
+    // ---- stage ------------------------------------------------------------
+    CUB(c.arena.reserve(arena_bytes), "cudaMalloc(batch arena)");
+    char *dev = (char *)c.arena.ptr;
+    const size_t upload_end = arena_bytes;
+    CUB(pinned_reserve(c, upload_end), "cudaHostAlloc(batch staging)");
+    char *host = (char *)c.pinned;
+    for (int j = j0; j < j1; j++) {
+        const size_t es = jobs[j].dtype == ACCRQA_GB300_F32 ? 4 : 8;
+        char *dst = host + xoff[(size_t)(j - j0)];
+        std::memcpy(dst, jobs[j].x, (size_t)jobs[j].n * es);
+        std::memset(dst + (size_t)jobs[j].n * es, 0, ACCRQA_SERIES_PAD * es);
+    }
+    for (GroupPlan &gp : plans) {
+        for (accrqa_batch_job &d : gp.table) {
+            const Pass &p = passes[(size_t)d.pad_];
+            d.pad_ = 0;
+            d.x = dev + xoff[(size_t)(p.job - j0)];
+            d.counts = p.kind == ACCRQA_WALK_RR ? (uint64_t *)(dev + p.counts_off) : nullptr;
+            d.maxlen = p.kind != ACCRQA_WALK_RR ? (uint32_t *)(dev + p.maxlen_off) : nullptr;
+            d.hist = p.kind != ACCRQA_WALK_RR ? (uint64_t *)(dev + p.hist_off) : nullptr;
+        }
+        std::memcpy(host + gp.jobs_off, gp.table.data(), gp.table.size() * sizeof(accrqa_batch_job));
+        std::memcpy(host + gp.units_off, gp.units.data(), gp.units.size() * sizeof(accrqa_batch_unit));
+        std::memcpy(host + gp.ranges_off, gp.ranges.data(), gp.ranges.size() * sizeof(int32_t));
+        gp.L.d_jobs = dev + gp.jobs_off;
+        gp.L.d_units = dev + gp.units_off;
+        gp.L.d_warp_begin = (const int32_t *)(dev + gp.ranges_off);
+    }
+    // series and tables in two copies (the result region between them is zeroed)
+    CUB(cudaMemcpyAsync(dev, host, series_bytes, cudaMemcpyHostToDevice, c.stream),
+        "cudaMemcpy(batch series)");
+    if (arena_bytes > zero_end)
+        CUB(cudaMemcpyAsync(dev + zero_end, host + zero_end, arena_bytes - zero_end,
+                            cudaMemcpyHostToDevice, c.stream), "cudaMemcpy(batch tables)");
+    transfer_stats_add(series_bytes + (arena_bytes - zero_end), 0);
+    CUB(cudaMemsetAsync(dev + zero_begin, 0, zero_end - zero_begin, c.stream), "cudaMemset(batch)");
+
+    // ---- launch: every group on a side stream, captured as one graph ------
+    CUB(side_streams(c, kSideStreams), "cudaStreamCreate");
+    cudaEvent_t fork, join[kSideStreams];
+    CUB(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming), "cudaEventCreate");
+    for (int s = 0; s < kSideStreams; s++)
+        CUB(cudaEventCreateWithFlags(&join[s], cudaEventDisableTiming), "cudaEventCreate");
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    Accrqa_Error err = SUCCESS;
+    cudaError_t ce = cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal);
+    if (ce == cudaSuccess) {
+        cudaEventRecord(fork, c.stream);
+        const int ns = std::min<int>(kSideStreams, (int)plans.size());
+        for (int s = 0; s < ns; s++) cudaStreamWaitEvent(c.side[(size_t)s], fork, 0);
+        // largest groups first, round-robin over the side streams
+        std::vector<int> ord(plans.size());
+        for (size_t i = 0; i < ord.size(); i++) ord[i] = (int)i;
+        std::sort(ord.begin(), ord.end(), [&](int a, int b) {
+            return plans[(size_t)a].units.size() > plans[(size_t)b].units.size();
+        });
+        for (size_t i = 0; i < ord.size(); i++) {
+            const int e = accrqa_gb300_launch_batch(&plans[(size_t)ord[i]].L, c.side[i % (size_t)ns]);
+            if (e && err == SUCCESS) err = cuda_error((cudaError_t)e, "batched kernel launch");
+        }
+        for (int s = 0; s < ns; s++) {
+            cudaEventRecord(join[s], c.side[(size_t)s]);
+            cudaStreamWaitEvent(c.stream, join[s], 0);
+        }
+        ce = cudaStreamEndCapture(c.stream, &graph);
+    }
+    if (ce == cudaSuccess && err == SUCCESS) ce = cudaGraphInstantiate(&exec, graph, 0);
+    if (ce == cudaSuccess && err == SUCCESS) ce = cudaGraphLaunch(exec, c.stream);
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    cudaEventDestroy(fork);
+    for (int s = 0; s < kSideStreams; s++) cudaEventDestroy(join[s]);
+    if (err != SUCCESS) return err;
+    CUB(ce, "batch graph");
+
+    // ---- results ----------------------------------------------------------
+    std::vector<char> small(head_end - zero_begin);
+    if (head_end > zero_begin) {
+        CUB(cudaMemcpyAsync(small.data(), dev + zero_begin, head_end - zero_begin,
+                            cudaMemcpyDeviceToHost, c.stream), "cudaMemcpy(batch counts)");
+        transfer_stats_add(0, head_end - zero_begin);
+    }
+    CUB(cudaStreamSynchronize(c.stream), "batched kernels");
+    // histogram prefixes
+    std::vector<std::vector<uint64_t>> pref(passes.size());
+    std::vector<int64_t> plen(passes.size(), 0);
+    for (size_t i = 0; i < passes.size(); i++) {
+        const Pass &p = passes[i];
+        if (p.kind == ACCRQA_WALK_RR) continue;
+        const uint32_t *mx = (const uint32_t *)(small.data() + (p.maxlen_off - zero_begin));
+        uint32_t m = 0;
+        for (int k = 0; k < p.cnt; k++) m = std::max(m, mx[k]);
+        int64_t P = std::max<int64_t>((int64_t)m + 1, ACCRQA_BATCH_BINS);
+        P = std::min<int64_t>(P, p.nc + 1);
+        plen[i] = P;
+        pref[i].resize((size_t)P * p.cnt);
+        CUB(cudaMemcpy2DAsync(pref[i].data(), (size_t)P * 8, dev + p.hist_off, (size_t)(p.nc + 1) * 8,
+                              (size_t)P * 8, (size_t)p.cnt, cudaMemcpyDeviceToHost, c.stream),
+            "cudaMemcpy(batch histograms)");
+        transfer_stats_add(0, (size_t)P * 8 * p.cnt);
+    }
+    CUB(cudaStreamSynchronize(c.stream), "histogram copy");
+
+    for (size_t i = 0; i < passes.size(); i++) {
+        const Pass &p = passes[i];
+        const accrqa_gb300_series_job &J = jobs[p.job];
+        const bool f32 = J.dtype == ACCRQA_GB300_F32;
+        if (p.kind == ACCRQA_WALK_RR) {
+            const uint64_t *cnt = (const uint64_t *)(small.data() + (p.counts_off - zero_begin));
+            for (int k = 0; k < p.cnt; k++) {
+                const double rr = (double)cnt[k] / (double)(p.nc * p.nc);
+                if (f32) ((float *)J.rr_out)[p.k0 + k] = (float)rr;
+                else ((double *)J.rr_out)[p.k0 + k] = rr;
+            }
+            continue;
+        }
+        const bool is_det = p.kind == ACCRQA_WALK_DET;
+        const int lm = is_det ? J.lmin : J.vmin;
+        const bool full = J.calc_entr == 1 || lm >= 16;
+        const int64_t P = plen[i];
+        for (int k = 0; k < p.cnt; k++) {
+            std::vector<uint64_t> h(pref[i].begin() + (size_t)k * P, pref[i].begin() + (size_t)(k + 1) * P);
+            uint64_t last = 0;
+            if (is_det) {
+                for (auto &v : h) v = 2 * v;
+                if (P == p.nc + 1) h[(size_t)p.nc] += 1;
+                else last = 1;
+            }
+            LineHistogram lh(std::move(h), last, p.nc);
+            void *out = is_det ? J.det_out : J.lam_out;
+            if (f32) write_line_out<float>(out, p.k0 + k, lh, lm, full, is_det);
+            else write_line_out<double>(out, p.k0 + k, lh, lm, full, is_det);
+        }
+    }
+    return SUCCESS;
+}
+
+Accrqa_Error run_batch(const accrqa_gb300_series_job *jobs, int njobs) {
+    if (!jobs || njobs < 0) return ERR_MEM_ALLOC_FAILURE;
+    for (int j = 0; j < njobs; j++) {
+        Accrqa_Error e = check_job(jobs[j]);
+        if (e) return e;
+    }
+    if (njobs == 0) return SUCCESS;
+    Accrqa_Error err = SUCCESS;
+    Context *c = current_context(&err);
+    if (!c) return err;
+    std::lock_guard<std::mutex> g(c->mu);
+    // sub-batches bounded by device memory: histograms dominate
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+        cudaGetLastError();
+        free_b = (size_t)4 << 30;
+    }
+    const size_t budget = std::min(free_b / 3, (size_t)16 << 30);
+    int j0 = 0;
+    while (j0 < njobs) {
+        size_t need = 0;
+        int j1 = j0;
+        while (j1 < njobs) {
+            const accrqa_gb300_series_job &J = jobs[j1];
+            const int64_t nc = J.n - (int64_t)(J.emb - 1) * J.tau;
+            const size_t es = J.dtype == ACCRQA_GB300_F32 ? 4 : 8;
+            size_t b = (size_t)(J.n + ACCRQA_SERIES_PAD) * es + 4096;
+            const int lines = (J.det_out ? 1 : 0) + (J.lam_out ? 1 : 0);
+            b += (size_t)lines * (size_t)J.nthr * (size_t)(nc + 1) * 8;
+            b += (size_t)(nc / 32 + 2) * 16;   // units
+            if (j1 > j0 && need + b > budget) break;
+            need += b;
+            j1++;
+        }
+        if ((err = run_batch_part(*c, jobs, j0, j1))) return err;
+        j0 = j1;
+    }
+    return SUCCESS;
+}
+
+}  // namespace accrqa

@@ -101,3 +101,29 @@ extern "C" int accrqa_gb300_launch_rp(const void *d_x, int32_t dtype, int32_t no
     }
     return (int)e;
 }
+
+namespace accrqa {
+cudaError_t batch_rr(const accrqa_batch_launch &, cudaStream_t, int *);
+cudaError_t batch_det(const accrqa_batch_launch &, cudaStream_t, int *);
+cudaError_t batch_lam(const accrqa_batch_launch &, cudaStream_t, int *);
+
+static cudaError_t batch_call(const accrqa_batch_launch *L, cudaStream_t st, int *w) {
+    if (!L) return cudaErrorInvalidValue;
+    switch (L->kind) {
+        case ACCRQA_WALK_RR: return batch_rr(*L, st, w);
+        case ACCRQA_WALK_DET: return batch_det(*L, st, w);
+        case ACCRQA_WALK_LAM: return batch_lam(*L, st, w);
+        default: return cudaErrorInvalidValue;
+    }
+}
+}  // namespace accrqa
+
+extern "C" int accrqa_gb300_launch_batch(const accrqa_batch_launch *L, void *stream) {
+    return (int)accrqa::batch_call(L, (cudaStream_t)stream, nullptr);
+}
+
+extern "C" int accrqa_gb300_batch_warps(const accrqa_batch_launch *L) {
+    int w = 0;
+    if (accrqa::batch_call(L, nullptr, &w) != cudaSuccess) return 0;
+    return w;
+}

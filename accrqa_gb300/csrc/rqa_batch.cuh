@@ -1,0 +1,200 @@
+// rqa_batch.cuh -- batched passes: many series (each with its own length,
+// tau, emb and thresholds) in one persistent launch.
+//
+// A launch serves one kernel shape (kind, dtype, norm, emb, threshold-slot
+// count); the host groups the passes of a batch by shape.  The work list is a
+// flat array of units (series, band or band pair) ordered by series; the host
+// splits it into one contiguous range per warp with equal total cells, so a
+// warp changes series only at the edges of its range.  Each warp keeps its own
+// shared-memory histogram bins and flushes them to the series' global
+// histogram when it moves on to the next series.
+#pragma once
+
+#include "engine_abi.h"
+#include "rqa_kernels.cuh"
+
+namespace accrqa {
+
+// Runs shorter than this go to the warp's shared-memory bins.
+constexpr int kBatchBins = 128;
+
+// One series' pass, in device memory (layout of accrqa_batch_job).
+typedef accrqa_batch_job BatchJob;
+
+struct BatchUnit {
+    int job;
+    int unit;   // band pair (RR, DET) or band (LAM) within the job
+};
+
+template <int NT>
+struct BatchSmem {
+    // per warp: bins [NT][kBatchBins], longest run [kMaxThrPerPass], run state 2*NT*32
+    static constexpr int kWarpWords = NT * kBatchBins + kMaxThrPerPass + 2 * NT * 32;
+    static constexpr size_t kBytes = (size_t)kWarpsPerCta * kWarpWords * sizeof(u32);
+};
+
+// Warp-level flush of a series' bins into its global histogram.
+template <int NT>
+__device__ __forceinline__ void batch_flush(u32 *bins, u32 *bmax, const BatchJob &j, int lane) {
+    __syncwarp();
+    for (int t = lane; t < j.nthr * kBatchBins; t += 32) {
+        const u32 c = bins[t];
+        if (c) {
+            const int k = t / kBatchBins, l = t - k * kBatchBins;
+            atomicAdd((u64 *)&j.hist[(long long)j.row[k] * j.hist_stride + l], (u64)c);
+        }
+    }
+    for (int t = lane; t < j.nthr; t += 32)
+        if (bmax[t]) atomicMax(&j.maxlen[j.row[t]], bmax[t]);
+    __syncwarp();
+    for (int t = lane; t < NT * kBatchBins; t += 32) bins[t] = 0;
+    if (lane < kMaxThrPerPass) bmax[lane] = 0;
+    __syncwarp();
+}
+
+// Sink whose short bins are the warp's own.
+struct WarpSink {
+    u32 *sh;
+    u32 *shmax;
+    u64 *gh;
+    long long stride;
+    const int *row;
+    __device__ __forceinline__ void emit(int k, u32 len) const {
+        if (len < (u32)kBatchBins) {
+            atomicAdd(&sh[k * kBatchBins + len], 1u);
+        } else {
+            atomicAdd(&gh[(long long)row[k] * stride + len], 1ull);
+            atomicMax(&shmax[k], len);
+        }
+    }
+};
+
+template <int KIND, typename T, int NORM, int EMB, int NT>
+__global__ void __launch_bounds__(kWarpsPerCta * 32)
+batch_walk(const BatchJob *__restrict__ jobs, const BatchUnit *__restrict__ units,
+           const int *__restrict__ warp_begin, int nwarps_total) {
+    extern __shared__ u32 smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    u32 *wbase = smem + warp * BatchSmem<NT>::kWarpWords;
+    u32 *bins = wbase;
+    u32 *bmax = bins + NT * kBatchBins;
+    u32 *runs = bmax + kMaxThrPerPass;
+    const LaneRuns r{runs, runs + NT * 32, lane};
+    for (int t = lane; t < NT * kBatchBins; t += 32) bins[t] = 0;
+    if (lane < kMaxThrPerPass) bmax[lane] = 0;
+    __syncwarp();
+
+    const int gw = blockIdx.x * kWarpsPerCta + warp;
+    if (gw >= nwarps_total) return;
+    const int u_begin = warp_begin[gw], u_end = warp_begin[gw + 1];
+
+    int cur = -1;
+    u64 keys[kMaxThrPerPass];
+    const BatchJob *jp = nullptr;
+    u64 total = 0;   // RR: lane k holds slot k's count for the current series
+    for (int u = u_begin; u < u_end; u++) {
+        const BatchUnit bu = units[u];
+        if (bu.job != cur) {
+            if (cur >= 0) {
+                if (KIND == ACCRQA_WALK_RR) {
+                    if (lane < jp->nthr && lane < NT && total) atomicAdd((u64 *)&jp->counts[jp->row[lane]], total);
+                    total = 0;
+                } else {
+                    batch_flush<NT>(bins, bmax, *jp, lane);
+                }
+            }
+            cur = bu.job;
+            jp = jobs + cur;
+#pragma unroll
+            for (int k = 0; k < kMaxThrPerPass; k++) keys[k] = jp->keys[k];
+        }
+        const T *__restrict__ x = (const T *)jp->x;
+        const long long nc = jp->nc, nbands = jp->nbands;
+        const long long tau = jp->tau;
+        const int emb = jp->emb;
+        if (KIND == ACCRQA_WALK_LAM) {
+            const long long band = bu.unit;
+            const long long i = band * 32 + lane;
+            const bool row_ok = i < nc;
+            T a[EMB > 0 ? EMB : 1];
+            load_lane_vec<T, EMB>(a, x + i, tau);
+            const WarpSink sink{bins, bmax, (u64 *)jp->hist, jp->hist_stride, jp->row};
+            runs_begin<NT>(r);
+            long long j0 = 0;
+            if (band * 32 + 31 < nc) {
+                for (; j0 + 32 <= nc; j0 += 32)
+                    lam_block<T, NORM, EMB, NT, false>(a, x + i, x + j0, tau, emb, 32, keys, r, sink);
+                if (j0 < nc)
+                    lam_block<T, NORM, EMB, NT, true>(a, x + i, x + j0, tau, emb, nc - j0, keys, r,
+                                                      sink);
+            } else {
+                for (; j0 < nc; j0 += 32)
+                    lam_block<T, NORM, EMB, NT, true>(a, x + i, x + j0, tau, emb,
+                                                      row_ok ? nc - j0 : 0, keys, r, sink);
+            }
+            runs_end<NT, WarpSink>(r, sink);
+        } else {
+#pragma unroll 1
+            for (int half = 0; half < 2; half++) {
+                const long long band = half == 0 ? bu.unit : nbands - 1 - bu.unit;
+                if (half == 1 && band == bu.unit) break;
+                if (KIND == ACCRQA_WALK_DET) {
+                    const WarpSink sink{bins, bmax, (u64 *)jp->hist, jp->hist_stride, jp->row};
+                    const long long d = 1 + band * 32 + lane;
+                    const long long len = nc - d;
+                    const long long wmin = nc - (band * 32 + 32);
+                    const long long wmax = nc - (band * 32 + 1);
+                    runs_begin<NT>(r);
+                    long long s0 = 0;
+                    for (; s0 + 32 <= wmin; s0 += 32)
+                        det_block<T, NORM, EMB, NT, false>(x + s0, x + s0 + d, tau, emb, 32, keys,
+                                                           r, sink);
+                    for (; s0 < wmax; s0 += 32)
+                        det_block<T, NORM, EMB, NT, true>(x + s0, x + s0 + d, tau, emb, len - s0,
+                                                          keys, r, sink);
+                    runs_end<NT, WarpSink>(r, sink);
+                } else {
+                    const long long i = band * 32 + lane;
+                    const bool row_ok = i < nc;
+                    T a[EMB > 0 ? EMB : 1];
+                    load_lane_vec<T, EMB>(a, x + i, tau);
+                    u32 up[NT], dg[NT];
+                    {
+                        const T v = cell_dist<T, NORM, EMB>(a, x + i, x + i, tau, emb);
+#pragma unroll
+                        for (int k = 0; k < NT; k++) {
+                            dg[k] = (row_ok && is_rec(v, keys[k])) ? 1u : 0u;
+                            up[k] = 0;
+                        }
+                    }
+                    const long long j0 = band * 32;
+                    const long long hi0 = nc - j0 < 32 ? nc - j0 : 32;
+                    rr_block<T, NORM, EMB, NT, true>(a, x + i, x + j0, tau, emb, lane + 1, hi0, keys,
+                                                     up);
+                    long long jb = j0 + 32;
+                    for (; jb + 32 <= nc; jb += 32)
+                        rr_block<T, NORM, EMB, NT, false>(a, x + i, x + jb, tau, emb, 0, 32, keys, up);
+                    if (jb < nc)
+                        rr_block<T, NORM, EMB, NT, true>(a, x + i, x + jb, tau, emb, 0, nc - jb, keys,
+                                                         up);
+#pragma unroll
+                    for (int k = 0; k < NT; k++) {
+                        u64 t = 2ull * (u64)(row_ok ? up[k] : 0u) + (u64)dg[k];
+#pragma unroll
+                        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xFFFFFFFFu, t, o);
+                        if (lane == k) total += t;
+                    }
+                }
+            }
+        }
+    }
+    if (cur >= 0) {
+        if (KIND == ACCRQA_WALK_RR) {
+            if (lane < jp->nthr && lane < NT && total) atomicAdd((u64 *)&jp->counts[jp->row[lane]], total);
+        } else {
+            batch_flush<NT>(bins, bmax, *jp, lane);
+        }
+    }
+}
+
+}  // namespace accrqa

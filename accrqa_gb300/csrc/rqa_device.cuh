@@ -198,8 +198,8 @@ struct HistSink {
 
 // Close the runs of one mask.  Runs that end inside the mask are emitted,
 // the run touching the top bit is carried.
-__device__ __forceinline__ void runs_of_mask(u32 m, u32 &carry, int k,
-                                             const HistSink &sink) {
+template <class Sink>
+__device__ __forceinline__ void runs_of_mask(u32 m, u32 &carry, int k, const Sink &sink) {
     if (m == 0u) {
         if (carry) {
             sink.emit(k, carry);

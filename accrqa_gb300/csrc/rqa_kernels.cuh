@@ -126,9 +126,9 @@ __device__ __forceinline__ void runs_begin(const LaneRuns &r) {
 // Close the runs of one 32-cell block for every slot.  Slots nest (slot 0 is
 // the widest threshold): when slot 0 has neither a recurrent cell nor an open
 // run, no slot has one; otherwise slots are visited until the first empty one.
-template <int NT>
+template <int NT, class Sink>
 __device__ __forceinline__ void close_block(const u32 (&m)[NT], const LaneRuns &r,
-                                            const HistSink &sink) {
+                                            const Sink &sink) {
     if ((walk_mask(m[0]) | r.c(0)) == 0u) return;
 #pragma unroll
     for (int k = 0; k < NT; k++) r.m(k) = m[k];
@@ -143,8 +143,8 @@ __device__ __forceinline__ void close_block(const u32 (&m)[NT], const LaneRuns &
 }
 
 // End of a line: every open run is complete.
-template <int NT>
-__device__ __forceinline__ void runs_end(const LaneRuns &r, const HistSink &sink) {
+template <int NT, class Sink>
+__device__ __forceinline__ void runs_end(const LaneRuns &r, const Sink &sink) {
 #pragma unroll 1
     for (int k = 0; k < NT; k++) {
         const u32 carry = r.c(k);
@@ -170,7 +170,7 @@ template <typename T, int NORM, int EMB, int NT, bool CHECK>
 __device__ __forceinline__ void rr_block(const T (&a)[EMB > 0 ? EMB : 1],
                                          const T *__restrict__ xi, const T *__restrict__ xj,
                                          long long tau, int emb, long long lo, long long hi,
-                                         const WalkArgs &p, u32 (&up)[NT]) {
+                                         const u64 (&keys)[kMaxThrPerPass], u32 (&up)[NT]) {
     u32 m[NT];
 #pragma unroll
     for (int k = 0; k < NT; k++) m[k] = 0;
@@ -182,7 +182,7 @@ __device__ __forceinline__ void rr_block(const T (&a)[EMB > 0 ? EMB : 1],
             v[c] = cell_dist<T, NORM, EMB>(a, xi, xj + g + c, tau, emb);
             if (CHECK && !(g + c >= lo && g + c < hi)) v[c] = never_value<T>();
         }
-        push_group<T, NT>(m, v, p.keys);
+        push_group<T, NT>(m, v, keys);
     }
 #pragma unroll
     for (int k = 0; k < NT; k++) up[k] += 32u - __popc(m[k]);
@@ -223,13 +223,13 @@ rr_rows(const __grid_constant__ WalkArgs p) {
             // first block: the columns j > i of the diagonal tile (j < nc)
             const long long j0 = band * 32;
             long long hi0 = nc - j0 < 32 ? nc - j0 : 32;
-            rr_block<T, NORM, EMB, NT, true>(a, x + i, x + j0, tau, p.emb, lane + 1, hi0, p, up);
+            rr_block<T, NORM, EMB, NT, true>(a, x + i, x + j0, tau, p.emb, lane + 1, hi0, p.keys, up);
             // full blocks: j > i for every lane, all columns inside the matrix
             long long jb = j0 + 32;
             for (; jb + 32 <= nc; jb += 32)
-                rr_block<T, NORM, EMB, NT, false>(a, x + i, x + jb, tau, p.emb, 0, 32, p, up);
+                rr_block<T, NORM, EMB, NT, false>(a, x + i, x + jb, tau, p.emb, 0, 32, p.keys, up);
             if (jb < nc)
-                rr_block<T, NORM, EMB, NT, true>(a, x + i, x + jb, tau, p.emb, 0, nc - jb, p, up);
+                rr_block<T, NORM, EMB, NT, true>(a, x + i, x + jb, tau, p.emb, 0, nc - jb, p.keys, up);
 #pragma unroll
             for (int k = 0; k < NT; k++) {
                 u64 t = 2ull * (u64)(row_ok ? up[k] : 0u) + (u64)dg[k];
@@ -248,12 +248,12 @@ rr_rows(const __grid_constant__ WalkArgs p) {
 // The histogram written here is the raw upper-triangle histogram; doubling
 // and the line of identity are applied by the host.
 // ---------------------------------------------------------------------------
-template <typename T, int NORM, int EMB, int NT, bool CHECK>
+template <typename T, int NORM, int EMB, int NT, bool CHECK, class Sink>
 __device__ __forceinline__ void det_block(const T *__restrict__ xs,
                                           const T *__restrict__ xsd,
                                           long long tau, int emb, long long rem,
-                                          const WalkArgs &p, const LaneRuns &r,
-                                          const HistSink &sink) {
+                                          const u64 (&keys)[kMaxThrPerPass], const LaneRuns &r,
+                                          const Sink &sink) {
     u32 m[NT];
 #pragma unroll
     for (int k = 0; k < NT; k++) m[k] = 0;
@@ -265,9 +265,9 @@ __device__ __forceinline__ void det_block(const T *__restrict__ xs,
             v[c] = cell_dist_mem<T, NORM, EMB>(xs + g + c, xsd + g + c, tau, emb);
             if (CHECK && (long long)(g + c) >= rem) v[c] = never_value<T>();
         }
-        push_group<T, NT>(m, v, p.keys);
+        push_group<T, NT>(m, v, keys);
     }
-    close_block<NT>(m, r, sink);
+    close_block<NT, Sink>(m, r, sink);
 }
 
 template <typename T, int NORM, int EMB, int NT>
@@ -300,12 +300,12 @@ det_diags(const __grid_constant__ WalkArgs p) {
             runs_begin<NT>(r);
             long long s0 = 0;
             for (; s0 + 32 <= wmin; s0 += 32)
-                det_block<T, NORM, EMB, NT, false>(x + s0, x + s0 + d, tau, p.emb, 32, p, r,
+                det_block<T, NORM, EMB, NT, false>(x + s0, x + s0 + d, tau, p.emb, 32, p.keys, r,
                                                    sink);
             for (; s0 < wmax; s0 += 32)
                 det_block<T, NORM, EMB, NT, true>(x + s0, x + s0 + d, tau, p.emb, len - s0,
-                                                  p, r, sink);
-            runs_end<NT>(r, sink);
+                                                  p.keys, r, sink);
+            runs_end<NT, HistSink>(r, sink);
         }
     }
     hist_smem_flush(sh, shmax, p);
@@ -316,13 +316,13 @@ det_diags(const __grid_constant__ WalkArgs p) {
 // columns j = 0 .. nc-1, 32 at a time.  Every row has nc cells, so plain
 // band striding is balanced.
 // ---------------------------------------------------------------------------
-template <typename T, int NORM, int EMB, int NT, bool CHECK>
+template <typename T, int NORM, int EMB, int NT, bool CHECK, class Sink>
 __device__ __forceinline__ void lam_block(const T (&a)[EMB > 0 ? EMB : 1],
                                           const T *__restrict__ xi,
                                           const T *__restrict__ xj,
                                           long long tau, int emb, long long rem,
-                                          const WalkArgs &p, const LaneRuns &r,
-                                          const HistSink &sink) {
+                                          const u64 (&keys)[kMaxThrPerPass], const LaneRuns &r,
+                                          const Sink &sink) {
     u32 m[NT];
 #pragma unroll
     for (int k = 0; k < NT; k++) m[k] = 0;
@@ -334,9 +334,9 @@ __device__ __forceinline__ void lam_block(const T (&a)[EMB > 0 ? EMB : 1],
             v[c] = cell_dist<T, NORM, EMB>(a, xi, xj + g + c, tau, emb);
             if (CHECK && (long long)(g + c) >= rem) v[c] = never_value<T>();
         }
-        push_group<T, NT>(m, v, p.keys);
+        push_group<T, NT>(m, v, keys);
     }
-    close_block<NT>(m, r, sink);
+    close_block<NT, Sink>(m, r, sink);
 }
 
 template <typename T, int NORM, int EMB, int NT>
@@ -368,16 +368,16 @@ lam_rows(const __grid_constant__ WalkArgs p) {
         // last, partial band the rows past nc see only never-recurrent cells.
         if (band * 32 + 31 < nc) {
             for (; j0 + 32 <= nc; j0 += 32)
-                lam_block<T, NORM, EMB, NT, false>(a, x + i, x + j0, tau, p.emb, 32, p, r, sink);
+                lam_block<T, NORM, EMB, NT, false>(a, x + i, x + j0, tau, p.emb, 32, p.keys, r, sink);
             if (j0 < nc)
-                lam_block<T, NORM, EMB, NT, true>(a, x + i, x + j0, tau, p.emb, nc - j0, p, r,
+                lam_block<T, NORM, EMB, NT, true>(a, x + i, x + j0, tau, p.emb, nc - j0, p.keys, r,
                                                   sink);
         } else {
             for (; j0 < nc; j0 += 32)
                 lam_block<T, NORM, EMB, NT, true>(a, x + i, x + j0, tau, p.emb,
-                                                  row_ok ? nc - j0 : 0, p, r, sink);
+                                                  row_ok ? nc - j0 : 0, p.keys, r, sink);
         }
-        runs_end<NT>(r, sink);
+        runs_end<NT, HistSink>(r, sink);
     }
     hist_smem_flush(sh, shmax, p);
 }

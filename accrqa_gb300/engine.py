@@ -125,6 +125,53 @@ def measures(hist, lmin: int, is_det: bool) -> np.ndarray:
 
 
 # ---------------------------------------------------------------------------
+# Many series in one submission
+# ---------------------------------------------------------------------------
+class SeriesJob(ctypes.Structure):
+    """accrqa_gb300_series_job (include/accrqa_gb300.h)."""
+    _fields_ = [("x", ctypes.c_void_p), ("n", ctypes.c_int64), ("dtype", ctypes.c_int32),
+                ("tau", ctypes.c_int32), ("emb", ctypes.c_int32), ("norm", ctypes.c_int32),
+                ("thresholds", ctypes.c_void_p), ("nthr", ctypes.c_int32),
+                ("lmin", ctypes.c_int32), ("vmin", ctypes.c_int32), ("calc_entr", ctypes.c_int32),
+                ("rr_out", ctypes.c_void_p), ("det_out", ctypes.c_void_p),
+                ("lam_out", ctypes.c_void_p)]
+
+
+def batch(jobs, measures=("rr", "det", "lam")):
+    """Run RR/DET/LAM for many series in one submission.
+
+    jobs: list of dicts with keys x (float32/float64 array), tau, emb, norm,
+    thresholds, and optional lmin (2), vmin (2), calc_entr (1).
+    Returns a list of dicts {"rr": [nthr], "det": [nthr, 5], "lam": [nthr, 5]}.
+    """
+    arr = (SeriesJob * len(jobs))()
+    keep, outs = [], []
+    for i, j in enumerate(jobs):
+        x = np.ascontiguousarray(j["x"])
+        thr = np.ascontiguousarray(j["thresholds"], dtype=x.dtype)
+        o = {}
+        if "rr" in measures:
+            o["rr"] = np.zeros(len(thr), dtype=x.dtype)
+        if "det" in measures:
+            o["det"] = np.zeros((len(thr), 5), dtype=x.dtype)
+        if "lam" in measures:
+            o["lam"] = np.zeros((len(thr), 5), dtype=x.dtype)
+        keep += [x, thr]
+        outs.append(o)
+        arr[i] = SeriesJob(x.ctypes.data, len(x), _dtype_code(x), j["tau"], j["emb"],
+                           _norm(j["norm"]), thr.ctypes.data, len(thr), j.get("lmin", 2),
+                           j.get("vmin", 2), j.get("calc_entr", 1),
+                           o["rr"].ctypes.data if "rr" in o else None,
+                           o["det"].ctypes.data if "det" in o else None,
+                           o["lam"].ctypes.data if "lam" in o else None)
+    f = _lib.handle().accrqa_gb300_batch
+    f.argtypes = [ctypes.POINTER(SeriesJob), ctypes.c_int32]
+    f.restype = ctypes.c_int
+    _check(f(arr, len(jobs)), "batch")
+    return outs
+
+
+# ---------------------------------------------------------------------------
 # Device-resident passes (pointers into device memory, enqueue only)
 # ---------------------------------------------------------------------------
 def rr_counts_dev(d_counts: int, d_x: int, dtype_code: int, n: int, tau: int, emb: int,

@@ -272,6 +272,37 @@ Accrqa_Error accrqa_gb300_lam_hist_dev(uint64_t *d_hist, int64_t stride,
                                        int32_t nthr, int32_t norm,
                                        void *stream);
 
+/* Many series in one submission.  Every job brings its own host series,
+ * length, tau, emb, norm and thresholds; rr_out / det_out / lam_out select
+ * the measures (NULL = not wanted) and receive them in the series dtype:
+ *   rr_out[k]            RR of threshold k
+ *   det_out[k*5 + 0..4]  {DET, L, Lmax, ENTR, RR} for minimal length lmin
+ *   lam_out[k*5 + 0..4]  {LAM, TT, TTmax, ENTR, RR} for minimal length vmin
+ * calc_entr follows accrqa_DET/accrqa_LAM (1, or lmin >= 16: all measures;
+ * otherwise Lmax/ENTR are NaN and RR is over (nc-1)^2).  Results equal those
+ * of one accrqa_RR/DET/LAM call per series.  No counterpart in the
+ * reference: the whole batch runs as one planned submission (one upload, one
+ * CUDA graph of persistent launches grouped by kernel shape, one download).
+ * Synchronous. */
+typedef struct accrqa_gb300_series_job {
+    const void *x;
+    int64_t n;
+    int32_t dtype;
+    int32_t tau;
+    int32_t emb;
+    int32_t norm;
+    const void *thresholds;
+    int32_t nthr;
+    int32_t lmin;
+    int32_t vmin;
+    int32_t calc_entr;
+    void *rr_out;
+    void *det_out;
+    void *lam_out;
+} accrqa_gb300_series_job;
+
+Accrqa_Error accrqa_gb300_batch(const accrqa_gb300_series_job *jobs, int32_t njobs);
+
 /* Recurrence rate for callers that cannot allocate device memory.  No
  * counterpart in the reference: it exists for callers that may not call
  * cudaMalloc -- code running while a stream is captured into a CUDA graph,

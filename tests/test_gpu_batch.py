@@ -1,0 +1,71 @@
+"""Batched submission: many uneven series in one call, identical to plain calls.
+
+Every batch output (RR, DET, LAM for each series, both output conventions,
+float32 and float64, emb specialised and generic, more than 16 thresholds)
+must equal what the per-series public API returns, bit for bit, and the raw
+counts behind them must equal the oracle's.
+"""
+import numpy as np
+import pytest
+
+import accrqa_gb300 as A
+from accrqa_gb300 import engine, workloads
+
+pytestmark = pytest.mark.gpu
+
+
+def _jobs(seed, count):
+    rng = np.random.default_rng(seed)
+    gens = [workloads.logistic, workloads.lorenz_x, workloads.ar1, workloads.white]
+    jobs = []
+    for i in range(count):
+        n = int(np.exp(rng.uniform(np.log(60), np.log(3000))))
+        dt = np.float64 if i % 5 == 4 else np.float32
+        x = gens[i % 4](n, int(rng.integers(1 << 30))).astype(dt)
+        x = (x / np.std(x.astype(np.float64))).astype(dt)
+        tau = int(rng.integers(1, 5))
+        emb = int(rng.integers(1, 10))
+        if n - (emb - 1) * tau < 2:
+            emb = 1
+        nthr = int(rng.choice([1, 3, 8, 11, 20]))
+        thr = np.sort(rng.uniform(0.05, 1.2, nthr)).astype(dt)
+        jobs.append(dict(x=x, tau=tau, emb=emb, norm=int(rng.integers(1, 3)), thresholds=thr,
+                         lmin=int(rng.choice([1, 2, 3, 17])), vmin=int(rng.choice([2, 4])),
+                         calc_entr=int(rng.integers(0, 2))))
+    return jobs
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_batch_equals_plain_calls(gpu, seed):
+    jobs = _jobs(seed, 40)
+    outs = engine.batch(jobs)
+    for j, o in zip(jobs, outs):
+        x, thr = j["x"], j["thresholds"]
+        D = A.accrqaDistance("euclidean" if j["norm"] == 1 else "maximal")
+        t = np.array([j["tau"]], np.intc)
+        e = np.array([j["emb"]], np.intc)
+        rr = A.RR(x, t, e, thr, D, tidy_data=False).reshape(-1)
+        np.testing.assert_array_equal(o["rr"], rr)
+        det = A.DET(x, t, e, np.array([j["lmin"]], np.intc), thr, D,
+                    calculate_ENTR=bool(j["calc_entr"]), tidy_data=False).reshape(-1, 5)
+        np.testing.assert_array_equal(o["det"], det)
+        lam = A.LAM(x, t, e, np.array([j["vmin"]], np.intc), thr, D,
+                    calculate_ENTR=bool(j["calc_entr"]), tidy_data=False).reshape(-1, 5)
+        np.testing.assert_array_equal(o["lam"], lam)
+
+
+def test_batch_counts_match_oracle(gpu, oracle_mod):
+    jobs = _jobs(7, 12)
+    outs = engine.batch(jobs, measures=("rr",))
+    for j, o in zip(jobs, outs):
+        nc = len(j["x"]) - (j["emb"] - 1) * j["tau"]
+        cnt = oracle_mod.rr_counts(j["x"], j["tau"], j["emb"], j["thresholds"], j["norm"])
+        np.testing.assert_array_equal(o["rr"], oracle_mod.rr_output(cnt, nc, j["x"].dtype))
+        assert "det" not in o
+
+
+def test_batch_rejects_bad_job(gpu):
+    jobs = _jobs(3, 2)
+    jobs[1]["tau"] = 0
+    with pytest.raises(engine.EngineError):
+        engine.batch(jobs)

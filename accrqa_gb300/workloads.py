@@ -53,6 +53,30 @@ def white(n: int, seed: int) -> np.ndarray:
     return np.random.default_rng(seed).standard_normal(n)
 
 
+def uneven_batch(count: int = 512, seed: int = 4, n_lo: int = 1000, n_hi: int = 64000,
+                 nthr: int = 8):
+    """The uneven batched workload: `count` series with lengths log-uniform in
+    [n_lo, n_hi], each a seeded mix (random convex weights) of z-scored
+    logistic-map, Lorenz-x and AR(1) series, float32; per series a random
+    tau in 1..4, emb in 2..8, norm Euclidean or maximal, and `nthr`
+    thresholds linearly spaced over 0.1..1.0 of the series' std."""
+    rng = np.random.default_rng(seed)
+    jobs = []
+    for i in range(count):
+        n = int(np.exp(rng.uniform(np.log(n_lo), np.log(n_hi))))
+        s = int(rng.integers(1 << 30))
+        parts = [logistic(n, s), lorenz_x(n, s + 1, transient=1000), ar1(n, s + 2)]
+        w = rng.dirichlet([1.0, 1.0, 1.0])
+        x = sum(wk * (p - p.mean()) / p.std() for wk, p in zip(w, parts))
+        x = x.astype(np.float32)
+        sd = float(np.std(x.astype(np.float64)))
+        jobs.append(dict(x=x, tau=int(rng.integers(1, 5)), emb=int(rng.integers(2, 9)),
+                         norm=int(rng.integers(1, 3)),
+                         thresholds=(np.linspace(0.1, 1.0, nthr) * sd).astype(np.float32),
+                         lmin=2, vmin=2, calc_entr=1))
+    return jobs
+
+
 def ar1(n: int, seed: int, phi: float = 0.95) -> np.ndarray:
     e = np.random.default_rng(seed).standard_normal(n)
     out = np.empty(n)

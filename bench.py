@@ -322,6 +322,8 @@ def run_ours(args):
                     for k, v in per_kind.items()},
         "clocks": clk,
     }
+    if rank == 0 and not args.skip_batched:
+        line["batched"] = batched_section(args)
     if rank == 0 and not args.no_cpu_baseline:
         log("cpu baseline")
         line["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
@@ -330,6 +332,58 @@ def run_ours(args):
         print(json.dumps(line), flush=True)
     if ws > 1:
         dist.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+# Batched uneven workload: one submission vs one plain call per series
+# ---------------------------------------------------------------------------
+def batched_section(args):
+    """512 series of log-uniform length in [1000, 64000] (seeded mixes of
+    logistic, Lorenz-x and AR(1)), random tau/emb/norm, 8 thresholds, RR +
+    DET + LAM with lmin = vmin = 2: the batched entry point against 512
+    triples of plain public-API calls, both on host buffers end to end, and a
+    check that every output is identical."""
+    import accrqa_gb300 as A
+    from accrqa_gb300 import engine, workloads
+
+    log("batched: generating the uneven workload")
+    jobs = workloads.uneven_batch(args.batch_series)
+    cells = 0
+    for j in jobs:
+        nc = len(j["x"]) - (j["emb"] - 1) * j["tau"]
+        cells += nc * nc * len(j["thresholds"]) * 3
+    engine.batch(jobs[:8])   # warm-up of the kernel shapes
+    times = []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        outs = engine.batch(jobs)
+        times.append(time.perf_counter() - t0)
+    t_batch = min(times)
+    log(f"batched: {t_batch:.3f} s")
+
+    def plain(j):
+        D = A.accrqaDistance("euclidean" if j["norm"] == 1 else "maximal")
+        t = np.array([j["tau"]], np.intc)
+        e = np.array([j["emb"]], np.intc)
+        lm = np.array([2], np.intc)
+        return (A.RR(j["x"], t, e, j["thresholds"], D, tidy_data=False).reshape(-1),
+                A.DET(j["x"], t, e, lm, j["thresholds"], D, tidy_data=False).reshape(-1, 5),
+                A.LAM(j["x"], t, e, lm, j["thresholds"], D, tidy_data=False).reshape(-1, 5))
+
+    for j in jobs[:8]:
+        plain(j)
+    t0 = time.perf_counter()
+    ref = [plain(j) for j in jobs]
+    t_plain = time.perf_counter() - t0
+    log(f"plain: {t_plain:.3f} s")
+    same = all(np.array_equal(o["rr"], r[0]) and np.array_equal(o["det"], r[1], equal_nan=True)
+               and np.array_equal(o["lam"], r[2], equal_nan=True) for o, r in zip(outs, ref))
+    return {"workload": f"{len(jobs)} uneven series (1e3..6.4e4 log-uniform, mixed generators), "
+                        "tau 1..4, emb 2..8, E/M norm, 8 thresholds, RR+DET+LAM, fp32",
+            "value": cells / t_batch, "unit": "cells/s", "seconds": t_batch,
+            "plain_value": cells / t_plain, "plain_seconds": t_plain,
+            "speedup_vs_plain": t_plain / t_batch, "identical_results": bool(same),
+            "cells": cells}
 
 
 # ---------------------------------------------------------------------------
@@ -460,6 +514,8 @@ def main(argv=None):
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--skip-batched", action="store_true")
+    ap.add_argument("--batch-series", type=int, default=512)
     args = ap.parse_args(argv)
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

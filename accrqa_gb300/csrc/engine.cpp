@@ -161,6 +161,23 @@ Context *current_context(Accrqa_Error *err) {
     return g_ctx[dev];
 }
 
+Context *context_create(Accrqa_Error *err) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) {
+        *err = cuda_error(e, "cudaGetDevice");
+        return nullptr;
+    }
+    std::unique_ptr<Context> c(new Context());
+    c->device = dev;
+    e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        *err = cuda_error(e, "cudaStreamCreate");
+        return nullptr;
+    }
+    return c.release();
+}
+
 // ===========================================================================
 // Threshold keys
 // ===========================================================================

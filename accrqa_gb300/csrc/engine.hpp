@@ -124,6 +124,14 @@ Accrqa_Error run_rp(OUT *out, const T *x, size_t n, int tau, int emb, T thr,
 
 // Many series in one submission (accrqa_gb300_batch).
 Accrqa_Error run_batch(const accrqa_gb300_series_job *jobs, int njobs);
+// The same on a given context, in sub-batches of at most `budget` device bytes.
+Accrqa_Error run_batch_in(Context &c, const accrqa_gb300_series_job *jobs, int njobs,
+                          size_t budget);
+// Device bytes one job of a batch needs (series, histograms, work units).
+size_t batch_job_bytes(const accrqa_gb300_series_job &job);
+Accrqa_Error check_batch_job(const accrqa_gb300_series_job &job);
+// A context that is not the device's shared one (for server workers).
+Context *context_create(Accrqa_Error *err);
 
 // Raw results for the engine C ABI (full-convention histograms).
 template <typename T>

@@ -403,6 +403,37 @@ static Accrqa_Error run_batch_part(Context &c, const accrqa_gb300_series_job *jo
     return SUCCESS;
 }
 
+size_t batch_job_bytes(const accrqa_gb300_series_job &J) {
+    const int64_t nc = J.n - (int64_t)(J.emb - 1) * J.tau;
+    const size_t es = J.dtype == ACCRQA_GB300_F32 ? 4 : 8;
+    size_t b = (size_t)(J.n + ACCRQA_SERIES_PAD) * es + 4096;
+    const int lines = (J.det_out ? 1 : 0) + (J.lam_out ? 1 : 0);
+    b += (size_t)lines * (size_t)J.nthr * (size_t)(nc + 1) * 8;
+    b += (size_t)(nc / 32 + 2) * 16;   // units
+    return b;
+}
+
+Accrqa_Error check_batch_job(const accrqa_gb300_series_job &j) { return check_job(j); }
+
+Accrqa_Error run_batch_in(Context &c, const accrqa_gb300_series_job *jobs, int njobs,
+                          size_t budget) {
+    Accrqa_Error err = SUCCESS;
+    int j0 = 0;
+    while (j0 < njobs) {
+        size_t need = 0;
+        int j1 = j0;
+        while (j1 < njobs) {
+            const size_t b = batch_job_bytes(jobs[j1]);
+            if (j1 > j0 && need + b > budget) break;
+            need += b;
+            j1++;
+        }
+        if ((err = run_batch_part(c, jobs, j0, j1))) return err;
+        j0 = j1;
+    }
+    return SUCCESS;
+}
+
 Accrqa_Error run_batch(const accrqa_gb300_series_job *jobs, int njobs) {
     if (!jobs || njobs < 0) return ERR_MEM_ALLOC_FAILURE;
     for (int j = 0; j < njobs; j++) {
@@ -420,27 +451,7 @@ Accrqa_Error run_batch(const accrqa_gb300_series_job *jobs, int njobs) {
         cudaGetLastError();
         free_b = (size_t)4 << 30;
     }
-    const size_t budget = std::min(free_b / 3, (size_t)16 << 30);
-    int j0 = 0;
-    while (j0 < njobs) {
-        size_t need = 0;
-        int j1 = j0;
-        while (j1 < njobs) {
-            const accrqa_gb300_series_job &J = jobs[j1];
-            const int64_t nc = J.n - (int64_t)(J.emb - 1) * J.tau;
-            const size_t es = J.dtype == ACCRQA_GB300_F32 ? 4 : 8;
-            size_t b = (size_t)(J.n + ACCRQA_SERIES_PAD) * es + 4096;
-            const int lines = (J.det_out ? 1 : 0) + (J.lam_out ? 1 : 0);
-            b += (size_t)lines * (size_t)J.nthr * (size_t)(nc + 1) * 8;
-            b += (size_t)(nc / 32 + 2) * 16;   // units
-            if (j1 > j0 && need + b > budget) break;
-            need += b;
-            j1++;
-        }
-        if ((err = run_batch_part(*c, jobs, j0, j1))) return err;
-        j0 = j1;
-    }
-    return SUCCESS;
+    return run_batch_in(*c, jobs, njobs, std::min(free_b / 3, (size_t)16 << 30));
 }
 
 }  // namespace accrqa

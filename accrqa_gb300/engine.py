@@ -171,6 +171,79 @@ def batch(jobs, measures=("rr", "det", "lam")):
     return outs
 
 
+class Server:
+    """Continuous-batching request server (accrqa_gb300_server_*).
+
+    submit(job) queues one series (dict as for batch(); "measures" selects
+    any of "rr", "det", "lam") and returns a ticket; wait(ticket) returns
+    (outputs, latency_ms)."""
+
+    def __init__(self, workers: int = 2, hbm_fraction: float = 0.5):
+        lib = _lib.handle()
+        lib.accrqa_gb300_server_create.restype = ctypes.c_void_p
+        lib.accrqa_gb300_server_create.argtypes = [ctypes.c_int32, ctypes.c_double]
+        lib.accrqa_gb300_server_submit.restype = ctypes.c_int64
+        lib.accrqa_gb300_server_submit.argtypes = [ctypes.c_void_p, ctypes.POINTER(SeriesJob)]
+        lib.accrqa_gb300_server_wait.restype = ctypes.c_int
+        lib.accrqa_gb300_server_wait.argtypes = [ctypes.c_void_p, ctypes.c_int64,
+                                                 ctypes.POINTER(ctypes.c_double)]
+        lib.accrqa_gb300_server_stats.argtypes = [ctypes.c_void_p,
+                                                  ctypes.POINTER(ctypes.c_uint64),
+                                                  ctypes.POINTER(ctypes.c_uint64)]
+        lib.accrqa_gb300_server_destroy.argtypes = [ctypes.c_void_p]
+        self._lib = lib
+        self._h = lib.accrqa_gb300_server_create(workers, hbm_fraction)
+        if not self._h:
+            raise EngineError(8, "server_create")
+        self._pending = {}
+
+    def submit(self, job) -> int:
+        x = np.ascontiguousarray(job["x"])
+        thr = np.ascontiguousarray(job["thresholds"], dtype=x.dtype)
+        want = job.get("measures", ("rr", "det", "lam"))
+        o = {}
+        if "rr" in want:
+            o["rr"] = np.zeros(len(thr), dtype=x.dtype)
+        if "det" in want:
+            o["det"] = np.zeros((len(thr), 5), dtype=x.dtype)
+        if "lam" in want:
+            o["lam"] = np.zeros((len(thr), 5), dtype=x.dtype)
+        sj = SeriesJob(x.ctypes.data, len(x), _dtype_code(x), job["tau"], job["emb"],
+                       _norm(job["norm"]), thr.ctypes.data, len(thr), job.get("lmin", 2),
+                       job.get("vmin", 2), job.get("calc_entr", 1),
+                       o["rr"].ctypes.data if "rr" in o else None,
+                       o["det"].ctypes.data if "det" in o else None,
+                       o["lam"].ctypes.data if "lam" in o else None)
+        t = self._lib.accrqa_gb300_server_submit(self._h, ctypes.byref(sj))
+        if t < 0:
+            raise EngineError(int(-t), "server_submit")
+        self._pending[t] = o
+        return int(t)
+
+    def wait(self, ticket: int):
+        lat = ctypes.c_double(0.0)
+        e = self._lib.accrqa_gb300_server_wait(self._h, ticket, ctypes.byref(lat))
+        o = self._pending.pop(ticket)
+        _check(e, "server_wait")
+        return o, lat.value
+
+    def stats(self):
+        b, s = ctypes.c_uint64(), ctypes.c_uint64()
+        self._lib.accrqa_gb300_server_stats(self._h, ctypes.byref(b), ctypes.byref(s))
+        return int(b.value), int(s.value)
+
+    def close(self):
+        if self._h:
+            self._lib.accrqa_gb300_server_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
 # ---------------------------------------------------------------------------
 # Device-resident passes (pointers into device memory, enqueue only)
 # ---------------------------------------------------------------------------

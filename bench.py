@@ -324,6 +324,8 @@ def run_ours(args):
     }
     if rank == 0 and not args.skip_batched:
         line["batched"] = batched_section(args)
+    if rank == 0 and not args.skip_served:
+        line["served"] = served_section(args)
     if rank == 0 and not args.no_cpu_baseline:
         log("cpu baseline")
         line["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
@@ -384,6 +386,113 @@ def batched_section(args):
             "plain_value": cells / t_plain, "plain_seconds": t_plain,
             "speedup_vs_plain": t_plain / t_batch, "identical_results": bool(same),
             "cells": cells}
+
+
+# ---------------------------------------------------------------------------
+# Served stream: Poisson arrivals, continuous batching vs sequential calls
+# ---------------------------------------------------------------------------
+def served_requests(count, seed=5):
+    """Requests of the served stream: length log-uniform in [2000, 256000],
+    float32 (float64 with probability 0.2), one measure of RR/DET/LAM, 1-16
+    thresholds (0.05-1.0 std), tau 1..4, emb 2..8, E/M norm."""
+    from accrqa_gb300 import workloads
+    rng = np.random.default_rng(seed)
+    gens = [workloads.logistic, workloads.ar1, workloads.white]
+    reqs = []
+    for i in range(count):
+        n = int(np.exp(rng.uniform(np.log(2000), np.log(256000))))
+        dt = np.float64 if rng.uniform() < 0.2 else np.float32
+        x = gens[i % 3](n, int(rng.integers(1 << 30)))
+        x = ((x - x.mean()) / x.std()).astype(dt)
+        nthr = int(rng.integers(1, 17))
+        reqs.append(dict(x=x, tau=int(rng.integers(1, 5)), emb=int(rng.integers(2, 9)),
+                         norm=int(rng.integers(1, 3)),
+                         thresholds=np.linspace(0.05, 1.0, nthr).astype(dt),
+                         measures=(str(rng.choice(["rr", "det", "lam"])),)))
+    return reqs
+
+
+def served_section(args):
+    """Serve a Poisson stream through the continuous-batching server and
+    through sequential plain calls (one FIFO worker), same requests, same
+    arrival times; report throughput and latency percentiles of both."""
+    import threading
+
+    import accrqa_gb300 as A
+    from accrqa_gb300 import engine
+
+    rate = args.serve_rate
+    reqs = served_requests(args.serve_requests)
+    rng = np.random.default_rng(6)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, len(reqs)))
+    cells = 0
+    for r in reqs:
+        nc = len(r["x"]) - (r["emb"] - 1) * r["tau"]
+        cells += nc * nc * len(r["thresholds"])
+
+    def plain(r):
+        D = A.accrqaDistance("euclidean" if r["norm"] == 1 else "maximal")
+        t = np.array([r["tau"]], np.intc)
+        e = np.array([r["emb"]], np.intc)
+        m = r["measures"][0]
+        if m == "rr":
+            return A.RR(r["x"], t, e, r["thresholds"], D, tidy_data=False)
+        f = A.DET if m == "det" else A.LAM
+        return f(r["x"], t, e, np.array([2], np.intc), r["thresholds"], D, tidy_data=False)
+
+    # warm the kernel shapes of both paths
+    for r in reqs[:6]:
+        plain(r)
+    with engine.Server(workers=args.serve_workers) as srv:
+        for r in reqs[:6]:
+            srv.wait(srv.submit(r))
+        log(f"served: {len(reqs)} requests at {rate} req/s")
+        lat = [0.0] * len(reqs)
+        tickets = [None] * len(reqs)
+        t0 = time.perf_counter()
+
+        def producer():
+            for i, r in enumerate(reqs):
+                dt = t0 + arrivals[i] - time.perf_counter()
+                if dt > 0:
+                    time.sleep(dt)
+                tickets[i] = srv.submit(r)
+
+        th = threading.Thread(target=producer)
+        th.start()
+        done = 0
+        while done < len(reqs):
+            if tickets[done] is None:
+                time.sleep(0.0005)
+                continue
+            _, lat[done] = srv.wait(tickets[done])
+            done += 1
+        th.join()
+        t_served = time.perf_counter() - t0
+        batches, served = srv.stats()
+    # sequential plain calls, FIFO, same arrival times
+    log("served: sequential plain calls")
+    seq_lat = []
+    t_free = 0.0
+    t0 = time.perf_counter()
+    for i, r in enumerate(reqs):
+        now = time.perf_counter() - t0
+        if now < arrivals[i]:
+            time.sleep(arrivals[i] - now)
+        start = time.perf_counter() - t0
+        plain(r)
+        end = time.perf_counter() - t0
+        seq_lat.append((end - arrivals[i]) * 1e3)
+        t_free = end
+    t_seq = t_free
+    p = lambda v, q: float(np.percentile(np.asarray(v), q))
+    return {"workload": f"{len(reqs)} requests, Poisson {rate} req/s, n log-uniform "
+                        "2e3..2.56e5, 20% fp64, one of RR/DET/LAM, 1-16 thresholds",
+            "rate_req_s": rate, "workers": args.serve_workers, "batches": batches,
+            "value": cells / t_served, "unit": "cells/s",
+            "p50_ms": p(lat, 50), "p99_ms": p(lat, 99),
+            "sequential_value": cells / t_seq, "sequential_p50_ms": p(seq_lat, 50),
+            "sequential_p99_ms": p(seq_lat, 99), "seconds": t_served, "sequential_seconds": t_seq}
 
 
 # ---------------------------------------------------------------------------
@@ -516,6 +625,10 @@ def main(argv=None):
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--skip-batched", action="store_true")
     ap.add_argument("--batch-series", type=int, default=512)
+    ap.add_argument("--skip-served", action="store_true")
+    ap.add_argument("--serve-rate", type=float, default=20.0)
+    ap.add_argument("--serve-requests", type=int, default=120)
+    ap.add_argument("--serve-workers", type=int, default=2)
     args = ap.parse_args(argv)
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

@@ -303,6 +303,26 @@ typedef struct accrqa_gb300_series_job {
 
 Accrqa_Error accrqa_gb300_batch(const accrqa_gb300_series_job *jobs, int32_t njobs);
 
+/* A request server with continuous batching (no counterpart in the
+ * reference).  `workers` threads, each with its own stream set and device
+ * arena, repeatedly take every queued request that fits their share of
+ * hbm_fraction of the free device memory and run them as one batch, so
+ * requests that arrive while others are on the GPU start as soon as a worker
+ * frees up and batches overlap on the device.
+ *   submit: copies the job's series and thresholds, returns a ticket >= 0 or
+ *           -Accrqa_Error; results go to the job's output buffers, which must
+ *           stay valid until the ticket is waited for.
+ *   wait  : blocks until the request is done; *latency_ms = completion time
+ *           minus submission time.  Each ticket is waited for once.
+ *   stats : batches run and requests served so far.
+ *   destroy: finishes the queued requests, then frees everything. */
+typedef struct accrqa_gb300_server accrqa_gb300_server;
+accrqa_gb300_server *accrqa_gb300_server_create(int32_t workers, double hbm_fraction);
+int64_t accrqa_gb300_server_submit(accrqa_gb300_server *s, const accrqa_gb300_series_job *job);
+Accrqa_Error accrqa_gb300_server_wait(accrqa_gb300_server *s, int64_t ticket, double *latency_ms);
+void accrqa_gb300_server_stats(accrqa_gb300_server *s, uint64_t *batches, uint64_t *served);
+void accrqa_gb300_server_destroy(accrqa_gb300_server *s);
+
 /* Recurrence rate for callers that cannot allocate device memory.  No
  * counterpart in the reference: it exists for callers that may not call
  * cudaMalloc -- code running while a stream is captured into a CUDA graph,

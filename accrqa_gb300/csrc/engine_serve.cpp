@@ -32,6 +32,7 @@ struct Request {
     accrqa_gb300_series_job job;
     std::vector<char> x, thr;   // owned copies of the inputs
     size_t bytes = 0;
+    double work = 0;   // cells x thresholds x measures, float64 weighted
     Clock::time_point t_submit, t_done;
     bool done = false;
     Accrqa_Error err = SUCCESS;
@@ -51,6 +52,7 @@ struct accrqa_gb300_server {
     bool stop = false;
     int device = 0;
     size_t budget = 0;   // device bytes per worker batch
+    double quantum = 0;  // estimated work (cell-thresholds) per worker batch
     std::vector<std::thread> workers;
     std::vector<accrqa::Context *> ctxs;
     uint64_t batches = 0, served = 0;
@@ -65,11 +67,18 @@ struct accrqa_gb300_server {
                 std::unique_lock<std::mutex> lk(mu);
                 cv_work.wait(lk, [&] { return stop || !pending.empty(); });
                 if (pending.empty()) return;   // stop requested and nothing left
+                // Admission: device bytes within the worker's share of free
+                // HBM, and estimated work within one batch quantum, so a
+                // large request runs on its own while small ones batch up.
                 size_t used = 0;
+                double work = 0.0;
                 while (!pending.empty()) {
                     Request *r = pending.front();
-                    if (!take.empty() && used + r->bytes > budget) break;
+                    if (!take.empty() &&
+                        (used + r->bytes > budget || work + r->work > quantum))
+                        break;
                     used += r->bytes;
+                    work += r->work;
                     take.push_back(r);
                     pending.pop_front();
                 }
@@ -112,6 +121,8 @@ Server *accrqa_gb300_server_create(int32_t workers, double hbm_fraction) {
         free_b = (size_t)8 << 30;
     }
     s->budget = (size_t)((double)free_b * hbm_fraction / workers);
+    // about 10 ms of float32 work on a GB300 (~1e13 cell-thresholds per second)
+    s->quantum = 1.0e11;
     for (int w = 0; w < workers; w++) {
         Context *c = context_create(&err);
         if (!c) return nullptr;
@@ -136,6 +147,12 @@ int64_t accrqa_gb300_server_submit(Server *s, const accrqa_gb300_series_job *job
     r->job.x = r->x.data();
     r->job.thresholds = r->thr.data();
     r->bytes = batch_job_bytes(r->job);
+    {
+        const double nc = (double)(job->n - (int64_t)(job->emb - 1) * job->tau);
+        const int measures = (job->rr_out ? 1 : 0) + (job->det_out ? 1 : 0) + (job->lam_out ? 2 : 0);
+        // float64 distances run on the FP64 pipe, far slower per cell
+        r->work = nc * nc * (double)job->nthr * measures * (job->dtype == ACCRQA_GB300_F64 ? 30.0 : 1.0);
+    }
     r->t_submit = std::chrono::steady_clock::now();
     std::lock_guard<std::mutex> lk(s->mu);
     if (s->stop) return -(int64_t)ERR_RUNTIME;

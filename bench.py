@@ -325,7 +325,7 @@ def run_ours(args):
     if rank == 0 and not args.skip_batched:
         line["batched"] = batched_section(args)
     if rank == 0 and not args.skip_served:
-        line["served"] = served_section(args)
+        line["served"] = [served_section(args, r) for r in args.serve_rates]
     if rank == 0 and not args.no_cpu_baseline:
         log("cpu baseline")
         line["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
@@ -412,7 +412,7 @@ def served_requests(count, seed=5):
     return reqs
 
 
-def served_section(args):
+def served_section(args, rate):
     """Serve a Poisson stream through the continuous-batching server and
     through sequential plain calls (one FIFO worker), same requests, same
     arrival times; report throughput and latency percentiles of both."""
@@ -421,7 +421,7 @@ def served_section(args):
     import accrqa_gb300 as A
     from accrqa_gb300 import engine
 
-    rate = args.serve_rate
+    rate = float(rate)
     reqs = served_requests(args.serve_requests)
     rng = np.random.default_rng(6)
     arrivals = np.cumsum(rng.exponential(1.0 / rate, len(reqs)))
@@ -474,6 +474,7 @@ def served_section(args):
     log("served: sequential plain calls")
     seq_lat = []
     t_free = 0.0
+    busy = 0.0
     t0 = time.perf_counter()
     for i, r in enumerate(reqs):
         now = time.perf_counter() - t0
@@ -483,6 +484,7 @@ def served_section(args):
         plain(r)
         end = time.perf_counter() - t0
         seq_lat.append((end - arrivals[i]) * 1e3)
+        busy += end - start
         t_free = end
     t_seq = t_free
     p = lambda v, q: float(np.percentile(np.asarray(v), q))
@@ -492,7 +494,8 @@ def served_section(args):
             "value": cells / t_served, "unit": "cells/s",
             "p50_ms": p(lat, 50), "p99_ms": p(lat, 99),
             "sequential_value": cells / t_seq, "sequential_p50_ms": p(seq_lat, 50),
-            "sequential_p99_ms": p(seq_lat, 99), "seconds": t_served, "sequential_seconds": t_seq}
+            "sequential_p99_ms": p(seq_lat, 99), "seconds": t_served, "sequential_seconds": t_seq,
+            "sequential_busy_seconds": busy}
 
 
 # ---------------------------------------------------------------------------
@@ -626,9 +629,9 @@ def main(argv=None):
     ap.add_argument("--skip-batched", action="store_true")
     ap.add_argument("--batch-series", type=int, default=512)
     ap.add_argument("--skip-served", action="store_true")
-    ap.add_argument("--serve-rate", type=float, default=20.0)
+    ap.add_argument("--serve-rates", type=lambda s: [float(v) for v in s.split(",")], default=[20.0, 60.0])
     ap.add_argument("--serve-requests", type=int, default=120)
-    ap.add_argument("--serve-workers", type=int, default=2)
+    ap.add_argument("--serve-workers", type=int, default=4)
     args = ap.parse_args(argv)
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

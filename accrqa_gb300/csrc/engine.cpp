@@ -507,17 +507,13 @@ static Accrqa_Error fetch_histograms(Context &c, int kind, const uint64_t *d_his
 // API-level drivers
 // ===========================================================================
 template <typename T>
-Accrqa_Error run_rr(T *out, const T *x, size_t n, const int *taus, int ntau,
-                    const int *embs, int nemb, const T *thr, int nthr, int norm) {
+Accrqa_Error run_rr_in(Context *c, T *out, const T *x, size_t n, const int *taus, int ntau,
+                       const int *embs, int nemb, const T *thr, int nthr, int norm) {
     Accrqa_Error err = check_norm(norm);
     if (err) return err;
     for (int a = 0; a < ntau; a++)
         for (int b = 0; b < nemb; b++)
             if ((err = check_combo(n, taus[a], embs[b]))) return err;
-    err = SUCCESS;
-    Context *c = current_context(&err);
-    if (!c) return err;
-    std::lock_guard<std::mutex> g(c->mu);
     const T *d_x = nullptr;
     if ((err = upload_series<T>(*c, x, (int64_t)n, &d_x))) return err;
     const size_t ncnt = (size_t)ntau * nemb * nthr;
@@ -550,9 +546,9 @@ Accrqa_Error run_rr(T *out, const T *x, size_t n, const int *taus, int ntau,
 }
 
 template <typename T>
-Accrqa_Error run_lines(int kind, T *out, const T *x, size_t n, const int *taus,
-                       int ntau, const int *embs, int nemb, const int *lmins,
-                       int nl, const T *thr, int nthr, int norm, int calc_entr) {
+Accrqa_Error run_lines_in(Context *c, int kind, T *out, const T *x, size_t n, const int *taus,
+                          int ntau, const int *embs, int nemb, const int *lmins,
+                          int nl, const T *thr, int nthr, int norm, int calc_entr) {
     Accrqa_Error err = check_norm(norm);
     if (err) return err;
     int lmin_max = 0;
@@ -570,10 +566,6 @@ Accrqa_Error run_lines(int kind, T *out, const T *x, size_t n, const int *taus,
     const bool full = calc_entr == 1 || lmin_max >= 16;
     const bool is_det = kind == ACCRQA_WALK_DET;
 
-    err = SUCCESS;
-    Context *c = current_context(&err);
-    if (!c) return err;
-    std::lock_guard<std::mutex> g(c->mu);
     const T *d_x = nullptr;
     if ((err = upload_series<T>(*c, x, (int64_t)n, &d_x))) return err;
 
@@ -642,6 +634,62 @@ Accrqa_Error run_lines(int kind, T *out, const T *x, size_t n, const int *taus,
             }
             trace("lines: combo %d measures done", q);
         }
+    }
+    return SUCCESS;
+}
+
+template <typename T>
+Accrqa_Error run_rr(T *out, const T *x, size_t n, const int *taus, int ntau,
+                    const int *embs, int nemb, const T *thr, int nthr, int norm) {
+    Accrqa_Error err = SUCCESS;
+    Context *c = current_context(&err);
+    if (!c) return err;
+    std::lock_guard<std::mutex> g(c->mu);
+    return run_rr_in<T>(c, out, x, n, taus, ntau, embs, nemb, thr, nthr, norm);
+}
+
+template <typename T>
+Accrqa_Error run_lines(int kind, T *out, const T *x, size_t n, const int *taus,
+                       int ntau, const int *embs, int nemb, const int *lmins,
+                       int nl, const T *thr, int nthr, int norm, int calc_entr) {
+    Accrqa_Error err = SUCCESS;
+    Context *c = current_context(&err);
+    if (!c) return err;
+    std::lock_guard<std::mutex> g(c->mu);
+    return run_lines_in<T>(c, kind, out, x, n, taus, ntau, embs, nemb, lmins, nl, thr, nthr,
+                           norm, calc_entr);
+}
+
+// One series job through the per-series path (reference output conventions).
+Accrqa_Error run_job_plain(Context &c, const accrqa_gb300_series_job &J) {
+    Accrqa_Error err = SUCCESS;
+    const int tau = J.tau, emb = J.emb, lmin = J.lmin, vmin = J.vmin;
+    if (J.dtype == ACCRQA_GB300_F32) {
+        const float *x = (const float *)J.x, *thr = (const float *)J.thresholds;
+        if (J.rr_out && (err = run_rr_in<float>(&c, (float *)J.rr_out, x, (size_t)J.n, &tau, 1,
+                                                &emb, 1, thr, J.nthr, J.norm)))
+            return err;
+        if (J.det_out && (err = run_lines_in<float>(&c, ACCRQA_WALK_DET, (float *)J.det_out, x,
+                                                    (size_t)J.n, &tau, 1, &emb, 1, &lmin, 1, thr,
+                                                    J.nthr, J.norm, J.calc_entr)))
+            return err;
+        if (J.lam_out && (err = run_lines_in<float>(&c, ACCRQA_WALK_LAM, (float *)J.lam_out, x,
+                                                    (size_t)J.n, &tau, 1, &emb, 1, &vmin, 1, thr,
+                                                    J.nthr, J.norm, J.calc_entr)))
+            return err;
+    } else {
+        const double *x = (const double *)J.x, *thr = (const double *)J.thresholds;
+        if (J.rr_out && (err = run_rr_in<double>(&c, (double *)J.rr_out, x, (size_t)J.n, &tau,
+                                                 1, &emb, 1, thr, J.nthr, J.norm)))
+            return err;
+        if (J.det_out && (err = run_lines_in<double>(&c, ACCRQA_WALK_DET, (double *)J.det_out,
+                                                     x, (size_t)J.n, &tau, 1, &emb, 1, &lmin, 1,
+                                                     thr, J.nthr, J.norm, J.calc_entr)))
+            return err;
+        if (J.lam_out && (err = run_lines_in<double>(&c, ACCRQA_WALK_LAM, (double *)J.lam_out,
+                                                     x, (size_t)J.n, &tau, 1, &emb, 1, &vmin, 1,
+                                                     thr, J.nthr, J.norm, J.calc_entr)))
+            return err;
     }
     return SUCCESS;
 }

@@ -122,6 +122,9 @@ template <typename T, typename OUT>
 Accrqa_Error run_rp(OUT *out, const T *x, size_t n, int tau, int emb, T thr,
                     int norm);
 
+// One series job through the per-series path, on a given context.
+Accrqa_Error run_job_plain(Context &c, const accrqa_gb300_series_job &job);
+
 // Many series in one submission (accrqa_gb300_batch).
 Accrqa_Error run_batch(const accrqa_gb300_series_job *jobs, int njobs);
 // The same on a given context, in sub-batches of at most `budget` device bytes.

@@ -3,9 +3,10 @@
 // Requests (one series each, any measure mix) are submitted from any thread
 // and queued with their arrival time.  K worker threads, each owning a private
 // engine context (stream, side streams, device arena, pinned staging), loop:
-// take every queued request that fits the worker's device-memory budget
-// (admission by free HBM, at least one request), run them as one batch
-// (engine_batch.cpp), complete them.  A request that arrives while batches are
+// take queued requests in arrival order while they fit the worker's
+// device-memory budget and one work quantum (at least one request), run them
+// as one batch (engine_batch.cpp) -- or, when only one was taken, through the
+// per-series path -- and complete them.  A request that arrives while batches are
 // on the GPU is picked up by the next free worker, so batches overlap on the
 // device and nobody waits for a fixed batching window.  Results are written
 // straight into the caller's output buffers, which must stay valid until the
@@ -83,10 +84,17 @@ struct accrqa_gb300_server {
                     pending.pop_front();
                 }
             }
-            std::vector<accrqa_gb300_series_job> jobs;
-            jobs.reserve(take.size());
-            for (Request *r : take) jobs.push_back(r->job);
-            const Accrqa_Error e = run_batch_in(*c, jobs.data(), (int)jobs.size(), budget);
+            // A request taken alone goes through the per-series path (no
+            // batch planning, graph or job tables to build for one series).
+            Accrqa_Error e;
+            if (take.size() == 1) {
+                e = run_job_plain(*c, take[0]->job);
+            } else {
+                std::vector<accrqa_gb300_series_job> jobs;
+                jobs.reserve(take.size());
+                for (Request *r : take) jobs.push_back(r->job);
+                e = run_batch_in(*c, jobs.data(), (int)jobs.size(), budget);
+            }
             const auto now = Clock::now();
             {
                 std::lock_guard<std::mutex> lk(mu);

@@ -74,6 +74,8 @@ def _declare(lib: ctypes.CDLL) -> None:
         f = getattr(lib, name)
         f.argtypes = [vp, i64, vp, vp, i32, i64, i32, i32, vp, i32, i32, vp]
         f.restype = ctypes.c_int
+    lib.accrqa_gb300_probe_fp32.argtypes = [i32, i32, ctypes.POINTER(ctypes.c_double)]
+    lib.accrqa_gb300_probe_fp32.restype = ctypes.c_int
 
 
 def last_error() -> str:

@@ -265,6 +265,11 @@ def LAM(input_data, tau_values, emb_values, vmin_values, threshold_values, dista
                   calculate_ENTR, comp_platform, tidy_data)
 
 
+# Bisection steps RR_target evaluates per RR call (2^4 - 1 = 15 thresholds,
+# one pass of the 16-threshold kernels).
+_RR_TARGET_DEPTH = 4
+
+
 def RR_target(input_data, tau: int, emb: int, target_RR: float, distance_type,
               epsilon: Optional[float] = 0.01,
               comp_platform: Optional[accrqaCompPlatform] = accrqaCompPlatform("nv_gpu"),
@@ -273,7 +278,7 @@ def RR_target(input_data, tau: int, emb: int, target_RR: float, distance_type,
     """Bisection for the threshold giving target_RR (src/accrqa/accrqa.py:470-594).
 
     Returns (threshold, RR).  The same bisection steps as the reference, on
-    float32 thresholds.
+    float32 thresholds, evaluated four steps per RR call (see below).
     """
     if type(distance_type) is not accrqaDistance:
         raise TypeError("distance must be an instance of accrqaDistance")
@@ -293,19 +298,52 @@ def RR_target(input_data, tau: int, emb: int, target_RR: float, distance_type,
         raise TypeError("threshold_min must be smaller then threshold_max.")
     taus = np.array([tau], dtype=np.intc)
     embs = np.array([emb], dtype=np.intc)
+
+    def rr_of(thresholds):
+        thr = np.asarray(thresholds, dtype=np.float32)
+        return RR(input_data, taus, embs, thr.astype(input_data.dtype), distance_type,
+                  comp_platform, tidy_data=False).flatten()
+
     mid = (threshold_max - threshold_min) / 2.0 + threshold_min
-    thr = np.array([threshold_min, mid, threshold_max], dtype=np.float32)
-    vals = RR(input_data, taus, embs, thr.astype(input_data.dtype), distance_type,
-              comp_platform, tidy_data=False).flatten()
+    vals = rr_of([threshold_min, mid, threshold_max])
     low_RR, hgh_RR = vals[0], vals[2]
     current_RR = vals[1]
-    for _ in range(1, max_iter + 1):
-        mid = (threshold_max - threshold_min) / 2.0 + threshold_min
-        thr = np.array([mid], dtype=np.float32)
-        current_RR = RR(input_data, taus, embs, thr.astype(input_data.dtype), distance_type,
-                        comp_platform, tidy_data=False).flatten()[0]
-        if abs(current_RR - target_RR) < epsilon:
-            return mid, current_RR
+    # The reference evaluates one midpoint per RR call.  Here the next `depth`
+    # bisection steps are evaluated speculatively in one call: every midpoint
+    # the search can reach from (threshold_min, threshold_max) within `depth`
+    # steps (2^depth - 1 thresholds, one 16-slot pass for depth 4), computed
+    # with the reference's float arithmetic; the walk down that tree then takes
+    # exactly the reference's decisions, so the result is the same.
+    iteration = 0
+    while iteration < max_iter:
+        depth = min(_RR_TARGET_DEPTH, max_iter - iteration)
+        nodes = [(threshold_min, threshold_max)]   # breadth-first, heap order
+        mids = []
+        for k in range((1 << depth) - 1):
+            lo, hi = nodes[k]
+            m = (hi - lo) / 2.0 + lo
+            mids.append(m)
+            if 2 * k + 2 < (1 << depth) - 1:
+                nodes.append((lo, m))   # child 2k+1: RR >= target, max = mid
+                nodes.append((m, hi))   # child 2k+2: RR < target, min = mid
+        rrs = rr_of(mids)
+        k = 0
+        for _ in range(depth):
+            iteration += 1
+            mid, current_RR = mids[k], rrs[k]
+            if abs(current_RR - target_RR) < epsilon:
+                return mid, current_RR
+            if (hgh_RR - low_RR) < epsilon:
+                return mid, current_RR
+            if current_RR < target_RR:
+                threshold_min = mid
+                k = 2 * k + 2
+            else:
+                threshold_max = mid
+                k = 2 * k + 1
+    print(f"Warning: Bisection search stopped after {max_iter} iterations")
+    mid = (threshold_max - threshold_min) / 2.0 + threshold_min
+    return mid, current_RR
         if (hgh_RR - low_RR) < epsilon:
             return mid, current_RR
         if current_RR < target_RR:

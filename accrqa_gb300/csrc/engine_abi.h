@@ -24,6 +24,17 @@ enum accrqa_dtype { ACCRQA_F32 = 0, ACCRQA_F64 = 1 };
 #define ACCRQA_SHORT_RUN_BINS 256
 #define ACCRQA_BATCH_BINS 128   /* short-run bins of the batched kernels */
 
+/* Kernel form of a float comparison key (accrqa_gb300_threshold_keys gives
+ * the largest passing value v, or -1.0f when none passes): the exclusive
+ * limit bits(key) + 1 (+inf above FLT_MAX), 0 when none passes, repeated in
+ * both 32-bit halves.  v < limit is the same decision as v <= key for every
+ * v >= +0, and the walk kernels evaluate it as the sign of v - limit. */
+static inline uint64_t accrqa_f32_limit_pair(uint64_t key) {
+    const uint32_t k = (uint32_t)key;
+    const uint32_t lim = (k & 0x80000000u) ? 0u : k + 1u;
+    return ((uint64_t)lim << 32) | (uint64_t)lim;
+}
+
 /* One kernel pass: one (series, tau, emb, norm) and up to 16 thresholds. */
 typedef struct accrqa_walk_desc {
     int32_t kind;            /* accrqa_walk_kind */
@@ -61,7 +72,8 @@ uint64_t accrqa_gb300_launch_count(void);
 /* ---- batched passes (many series per launch) ---------------------------- */
 
 /* One series' pass as the batched kernels read it (device memory).  Keys are
- * sorted by decreasing threshold, row[k] is the output row of slot k, padding
+ * in kernel form (float: accrqa_f32_limit_pair) and sorted by decreasing
+ * threshold, row[k] is the output row of slot k, padding
  * slots hold the never-recurrent key.  Same layout as accrqa::BatchJob. */
 typedef struct accrqa_batch_job {
     const void *x;

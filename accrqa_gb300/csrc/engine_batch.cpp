@@ -223,6 +223,7 @@ static Accrqa_Error run_batch_part(Context &c, const accrqa_gb300_series_job *jo
             const uint64_t never = J.dtype == ACCRQA_GB300_F32 ? 0xBF800000ull : 0ull;
             for (int k = 0; k < ACCRQA_MAX_THR_PER_PASS; k++) {
                 d.keys[k] = k < p.cnt ? raw[order[k]] : never;
+                if (J.dtype == ACCRQA_GB300_F32) d.keys[k] = accrqa_f32_limit_pair(d.keys[k]);
                 d.row[k] = k < p.cnt ? order[k] : 0;
             }
             d.hist_stride = p.nc + 1;

@@ -116,8 +116,8 @@ batch_walk(const BatchJob *__restrict__ jobs, const BatchUnit *__restrict__ unit
             const long long band = bu.unit;
             const long long i = band * 32 + lane;
             const bool row_ok = i < nc;
-            T a[EMB > 0 ? EMB : 1];
-            load_lane_vec<T, EMB>(a, x + i, tau);
+            LaneVec<T, EMB> a;
+            a.load(x + i, tau);
             const WarpSink sink{bins, bmax, (u64 *)jp->hist, jp->hist_stride, jp->row};
             runs_begin<NT>(r);
             long long j0 = 0;
@@ -156,14 +156,14 @@ batch_walk(const BatchJob *__restrict__ jobs, const BatchUnit *__restrict__ unit
                 } else {
                     const long long i = band * 32 + lane;
                     const bool row_ok = i < nc;
-                    T a[EMB > 0 ? EMB : 1];
-                    load_lane_vec<T, EMB>(a, x + i, tau);
+                    LaneVec<T, EMB> a;
+                    a.load(x + i, tau);
                     u32 up[NT], dg[NT];
                     {
-                        const T v = cell_dist<T, NORM, EMB>(a, x + i, x + i, tau, emb);
+                        const T v = cell_dist_mem<T, NORM, EMB>(x + i, x + i, tau, emb);
 #pragma unroll
                         for (int k = 0; k < NT; k++) {
-                            dg[k] = (row_ok && is_rec(v, keys[k])) ? 1u : 0u;
+                            dg[k] = (row_ok && is_rec_lim(v, keys[k])) ? 1u : 0u;
                             up[k] = 0;
                         }
                     }

@@ -15,7 +15,8 @@
 // Euclidean norm and the identity for the maximal norm.  Because both sqrt and
 // (t - .) are monotone, "v <= key" is the same decision, bit for bit.
 //   float : v <= key as a float compare; a threshold that is never met gets
-//           key = -1 (v >= +0 or NaN, so the compare is false).
+//           key = -1 (v >= +0 or NaN, so the compare is false).  The walk
+//           kernels receive the equivalent exclusive limit instead (below).
 //   double: the bit pattern of v (>= +0, or NaN) compared as an unsigned
 //           64-bit integer against an exclusive limit bits(key) + 1; a
 //           threshold that is never met gets limit 0.  NaN bit patterns lie
@@ -98,7 +99,7 @@ __device__ __forceinline__ T dist_step(T acc, T a, T b, bool first) {
     }
 }
 
-// Decision "v <= key" (see the file comment for the key encoding).
+// Decision with an inclusive key, "v <= key" (recurrence plots).
 __device__ __forceinline__ bool is_rec(float v, u64 key) {
     return v <= __uint_as_float((u32)key);
 }
@@ -106,73 +107,149 @@ __device__ __forceinline__ bool is_rec(double v, u64 key) {
     return (u64)__double_as_longlong(v) < key;
 }
 
-// Append one cell to every slot's mask: masks are shifted left and the new
-// cell enters at bit 0 as 1 when it is NOT recurrent.
-//   float : d = key - v on the FMA pipe; its sign bit is the answer (v <= key
-//           gives +0 or a positive d; a NaN v was mapped to +inf first) and
-//           one funnel shift moves it into the mask.
-//   double: an integer compare of the bit pattern against the limit.
-template <int NT>
-__device__ __forceinline__ void push_cell(u32 (&m)[NT], float v, const u64 (&keys)[kMaxThrPerPass]) {
-    v = fminf(v, __int_as_float(0x7f800000));
-#pragma unroll
-    for (int k = 0; k < NT; k++) {
-        const float d = __fsub_rn(__uint_as_float((u32)keys[k]), v);
-        m[k] = __funnelshift_l(__float_as_uint(d), m[k], 1);
-    }
+// The walk kernels take float keys as exclusive limits: lim = the next float
+// above the key (bits + 1; +inf above FLT_MAX), 0 when nothing passes, held
+// twice in the 64-bit slot so that it is a ready f32x2 operand.  Then
+//   d = v - lim  has its sign bit set  <=>  v < lim  <=>  v <= key,
+// and a NaN v (or inf - inf) gives the GPU's canonical, positive NaN: not
+// recurrent, as in the reference.  Double keys are exclusive limits already.
+__device__ __forceinline__ bool is_rec_lim(float v, u64 lim) {
+    return v < __uint_as_float((u32)lim);
 }
-template <int NT>
-__device__ __forceinline__ void push_cell(u32 (&m)[NT], double v, const u64 (&keys)[kMaxThrPerPass]) {
-    const u64 b = (u64)__double_as_longlong(v);
-#pragma unroll
-    for (int k = 0; k < NT; k++) m[k] = (m[k] << 1) | (b >= keys[k] ? 1u : 0u);
+__device__ __forceinline__ bool is_rec_lim(double v, u64 lim) {
+    return (u64)__double_as_longlong(v) < lim;
 }
 
-// Cells are pushed in groups of kGroup.  When no cell of a group passes the
-// widest threshold (slot 0), every mask just takes kGroup "not recurrent"
-// bits -- one operation per slot instead of two per slot and cell.
-constexpr int kGroup = 8;
+// ---------------------------------------------------------------------------
+// Packed float pairs for the f32x2 instructions of sm_100-family GPUs: two
+// cells in one 64-bit register (lo = first cell), each half computed and
+// rounded exactly as the scalar round-to-nearest instruction would.
+// ---------------------------------------------------------------------------
+typedef u64 f2;
 
-__device__ __forceinline__ bool group_any(const float (&v)[kGroup], u64 key0) {
-    float lo = v[0];
-#pragma unroll
-    for (int g = 1; g < kGroup; g++) lo = fminf(lo, v[g]);   // NaN-ignoring
-    return is_rec(lo, key0);
+__device__ __forceinline__ f2 pack2(float lo, float hi) {
+    f2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
 }
-__device__ __forceinline__ bool group_any(const double (&v)[kGroup], u64 key0) {
-    u64 lo = (u64)__double_as_longlong(v[0]);
-#pragma unroll
-    for (int g = 1; g < kGroup; g++) {
-        const u64 b = (u64)__double_as_longlong(v[g]);
-        lo = b < lo ? b : lo;
-    }
-    return lo < key0;
+__device__ __forceinline__ float lo_of(f2 v) { return __uint_as_float((u32)v); }
+__device__ __forceinline__ float hi_of(f2 v) { return __uint_as_float((u32)(v >> 32)); }
+__device__ __forceinline__ f2 sub2(f2 a, f2 b) {
+    f2 r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2 mul2(f2 a, f2 b) {
+    f2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2 add2(f2 a, f2 b) {
+    f2 r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
 }
 
-// The decision is taken for the whole warp (all lanes call this together): a
-// lane with nothing recurrent in a group that another lane needs simply pushes
-// its all-"not recurrent" bits through the per-cell path, which keeps the
-// warp on one path instead of serialising both.
-template <typename T, int NT>
-__device__ __forceinline__ void push_group(u32 (&m)[NT], const T (&v)[kGroup],
-                                           const u64 (&keys)[kMaxThrPerPass]) {
-    if (!__any_sync(0xFFFFFFFFu, group_any(v, keys[0]))) {
-#pragma unroll
-        for (int k = 0; k < NT; k++) m[k] = (m[k] << kGroup) | ((1u << kGroup) - 1u);
-    } else {
-#pragma unroll
-        for (int g = 0; g < kGroup; g++) push_cell<NT>(m, v[g], keys);
+// Distances of two cells from their operand pairs a[m], b[m] (m = 0..emb-1).
+// Euclidean: difference and square on the f32x2 pipe, the running sum in the
+// reference's order with scalar adds.  The sum stays scalar on purpose: the
+// code generator contracts a packed multiply feeding a packed add into a
+// fused multiply-add even when both carry .rn, which would round the square
+// and the sum once instead of twice (the oracle parity tests catch any such
+// change).  Maximal: the difference on the f32x2 pipe, |.| and the running
+// maximum per half.
+template <int NORM>
+struct Dist2 {
+    float al, ah;
+    __device__ __forceinline__ void step(f2 a, f2 b, bool first) {
+        const f2 d = sub2(a, b);
+        if (NORM == kNormEuclidean) {
+            const f2 sq = mul2(d, d);
+            al = first ? lo_of(sq) : __fadd_rn(al, lo_of(sq));
+            ah = first ? hi_of(sq) : __fadd_rn(ah, hi_of(sq));
+        } else {
+            al = fmaxf(first ? 0.0f : al, fabsf(lo_of(d)));
+            ah = fmaxf(first ? 0.0f : ah, fabsf(hi_of(d)));
+        }
     }
-}
+    __device__ __forceinline__ f2 value() const { return pack2(al, ah); }
+};
 
 // Value that is never recurrent (for cells past the end of a line).
 template <typename T> __device__ __forceinline__ T never_value();
 template <> __device__ __forceinline__ float never_value<float>() { return __int_as_float(0x7f800000); }
 template <> __device__ __forceinline__ double never_value<double>() { return __longlong_as_double(-1ll); }
 
-// Recurrent-cell mask in walk order (bit c = c-th pushed cell) from the
-// pushed "not recurrent" bits.
-__device__ __forceinline__ u32 walk_mask(u32 m) { return __brev(~m); }
+// ---------------------------------------------------------------------------
+// Masks.  Each slot keeps a 32-bit mask of the block's cells, pushed in walk
+// order (the first cell ends up in the top bit); a set bit is a recurrent
+// cell.  Cells are pushed in groups of kGroup.  When no lane of the warp has
+// a recurrent cell of the group at the widest threshold (slot 0), every mask
+// just shifts in kGroup zeros: one operation per slot instead of the compare
+// and push per slot and cell.  The decision is warp-wide (all lanes call the
+// group functions together), which keeps the warp on one path.
+// ---------------------------------------------------------------------------
+constexpr int kGroup = 8;
+
+// float: four cell pairs.  d = v - lim on the f32x2 pipe, then one funnel
+// shift per cell moves its sign bit (recurrent) into the mask.
+template <int NT>
+__device__ __forceinline__ void push_group(u32 (&m)[NT], const f2 (&v)[kGroup / 2],
+                                           const u64 (&keys)[kMaxThrPerPass]) {
+    f2 d0[kGroup / 2];
+    u64 any = 0;
+#pragma unroll
+    for (int q = 0; q < kGroup / 2; q++) {
+        d0[q] = sub2(v[q], keys[0]);
+        any |= d0[q];
+    }
+    const u32 signs = ((u32)any | (u32)(any >> 32)) >> 31;
+    if (!__any_sync(0xFFFFFFFFu, signs)) {
+#pragma unroll
+        for (int k = 0; k < NT; k++) m[k] <<= kGroup;
+        return;
+    }
+#pragma unroll
+    for (int q = 0; q < kGroup / 2; q++) {
+        m[0] = __funnelshift_l((u32)d0[q], m[0], 1);
+        m[0] = __funnelshift_l((u32)(d0[q] >> 32), m[0], 1);
+    }
+#pragma unroll
+    for (int k = 1; k < NT; k++) {
+#pragma unroll
+        for (int q = 0; q < kGroup / 2; q++) {
+            const f2 d = sub2(v[q], keys[k]);
+            m[k] = __funnelshift_l((u32)d, m[k], 1);
+            m[k] = __funnelshift_l((u32)(d >> 32), m[k], 1);
+        }
+    }
+}
+
+// double: an integer compare of the bit pattern against the limit.
+template <int NT>
+__device__ __forceinline__ void push_group(u32 (&m)[NT], const double (&v)[kGroup],
+                                           const u64 (&keys)[kMaxThrPerPass]) {
+    u64 lo = (u64)__double_as_longlong(v[0]);
+#pragma unroll
+    for (int g = 1; g < kGroup; g++) {
+        const u64 b = (u64)__double_as_longlong(v[g]);
+        lo = b < lo ? b : lo;
+    }
+    if (!__any_sync(0xFFFFFFFFu, lo < keys[0])) {
+#pragma unroll
+        for (int k = 0; k < NT; k++) m[k] <<= kGroup;
+        return;
+    }
+#pragma unroll
+    for (int g = 0; g < kGroup; g++) {
+        const u64 b = (u64)__double_as_longlong(v[g]);
+#pragma unroll
+        for (int k = 0; k < NT; k++) m[k] = (m[k] << 1) | (b < keys[k] ? 1u : 0u);
+    }
+}
+
+// Recurrent-cell mask in walk order (bit c = c-th pushed cell).
+__device__ __forceinline__ u32 walk_mask(u32 m) { return __brev(m); }
 
 // ---------------------------------------------------------------------------
 // Line-length bookkeeping.  A 32-bit mask holds 32 consecutive cells of one

@@ -34,28 +34,9 @@ namespace accrqa {
 constexpr int kWarpsPerCta = 4;
 constexpr int kSeriesPad = 128;
 
-// Distance between the register vector a[m] = x[i + m*tau] and the vector
-// starting at xj.  EMB = 0 is the generic instantiation (runtime emb, both
-// operands read from memory through xi).
-template <typename T, int NORM, int EMB>
-__device__ __forceinline__ T cell_dist(const T (&a)[EMB > 0 ? EMB : 1],
-                                       const T *__restrict__ xi,
-                                       const T *__restrict__ xj, long long tau,
-                                       int emb) {
-    T acc = T(0);
-    if (EMB > 0) {
-#pragma unroll
-        for (int m = 0; m < (EMB > 0 ? EMB : 1); m++)
-            acc = dist_step<T, NORM>(acc, a[m], __ldg(xj + m * tau), m == 0);
-    } else {
-        for (int m = 0; m < emb; m++)
-            acc = dist_step<T, NORM>(acc, __ldg(xi + m * tau), __ldg(xj + m * tau),
-                                     m == 0);
-    }
-    return acc;
-}
-
-// Distance with both operands read from memory.
+// Distance of one cell with both operands read from memory (scalar path:
+// the main-diagonal cell of the RR walk and the recurrence plot).  EMB = 0 is
+// the generic instantiation (runtime emb).
 template <typename T, int NORM, int EMB>
 __device__ __forceinline__ T cell_dist_mem(const T *__restrict__ xi,
                                            const T *__restrict__ xj,
@@ -74,13 +55,152 @@ __device__ __forceinline__ T cell_dist_mem(const T *__restrict__ xi,
     return acc;
 }
 
+// The lane's own embedded vector x[i + m*tau], m = 0..EMB-1, in registers;
+// for float as pairs (x, x) that meet two cells in one f32x2 instruction.
+// EMB = 0 (runtime emb) keeps nothing: its operands are read from memory.
 template <typename T, int EMB>
-__device__ __forceinline__ void load_lane_vec(T (&a)[EMB > 0 ? EMB : 1],
-                                              const T *__restrict__ xi,
-                                              long long tau) {
-    if (EMB > 0) {
+struct LaneVec {
+    T v[EMB > 0 ? EMB : 1];
+    __device__ __forceinline__ void load(const T *__restrict__ xi, long long tau) {
 #pragma unroll
-        for (int m = 0; m < (EMB > 0 ? EMB : 1); m++) a[m] = __ldg(xi + m * tau);
+        for (int m = 0; m < EMB; m++) v[m] = __ldg(xi + m * tau);
+    }
+};
+template <int EMB>
+struct LaneVec<float, EMB> {
+    f2 v[EMB > 0 ? EMB : 1];
+    __device__ __forceinline__ void load(const float *__restrict__ xi, long long tau) {
+#pragma unroll
+        for (int m = 0; m < EMB; m++) {
+            const float t = __ldg(xi + m * tau);
+            v[m] = pack2(t, t);
+        }
+    }
+};
+
+// The values of one group of kGroup cells: float as cell pairs.
+template <typename T> struct GroupOf;
+template <> struct GroupOf<float> { typedef f2 type[kGroup / 2]; };
+template <> struct GroupOf<double> { typedef double type[kGroup]; };
+
+__device__ __forceinline__ bool in_range(int c, long long lo, long long hi) {
+    return (long long)c >= lo && (long long)c < hi;
+}
+
+// Row walker: cells xj[g .. g+kGroup) against the lane's vector (row i).
+// With CHECK, cells outside [lo, hi) are never recurrent.
+template <int NORM, int EMB, bool CHECK>
+__device__ __forceinline__ void row_group(f2 (&v)[kGroup / 2], const LaneVec<float, EMB> &a,
+                                          const float *__restrict__ xi,
+                                          const float *__restrict__ xj, long long tau, int emb,
+                                          int g, long long lo, long long hi) {
+#pragma unroll
+    for (int q = 0; q < kGroup / 2; q++) {
+        const float *p = xj + g + 2 * q;
+        Dist2<NORM> d{0.0f, 0.0f};
+        if (EMB > 0) {
+#pragma unroll
+            for (int m = 0; m < (EMB > 0 ? EMB : 1); m++)
+                d.step(a.v[m], pack2(__ldg(p + m * tau), __ldg(p + 1 + m * tau)), m == 0);
+        } else {
+            for (int m = 0; m < emb; m++) {
+                const float t = __ldg(xi + m * tau);
+                d.step(pack2(t, t), pack2(__ldg(p + m * tau), __ldg(p + 1 + m * tau)), m == 0);
+            }
+        }
+        f2 r = d.value();
+        if (CHECK) {
+            const int c = g + 2 * q;
+            const bool ok0 = in_range(c, lo, hi), ok1 = in_range(c + 1, lo, hi);
+            r = pack2(ok0 ? lo_of(r) : never_value<float>(), ok1 ? hi_of(r) : never_value<float>());
+        }
+        v[q] = r;
+    }
+}
+template <int NORM, int EMB, bool CHECK>
+__device__ __forceinline__ void row_group(double (&v)[kGroup], const LaneVec<double, EMB> &a,
+                                          const double *__restrict__ xi,
+                                          const double *__restrict__ xj, long long tau, int emb,
+                                          int g, long long lo, long long hi) {
+#pragma unroll
+    for (int c = 0; c < kGroup; c++) {
+        double acc = 0.0;
+        if (EMB > 0) {
+#pragma unroll
+            for (int m = 0; m < (EMB > 0 ? EMB : 1); m++)
+                acc = dist_step<double, NORM>(acc, a.v[m], __ldg(xj + g + c + m * tau), m == 0);
+        } else {
+            for (int m = 0; m < emb; m++)
+                acc = dist_step<double, NORM>(acc, __ldg(xi + m * tau),
+                                              __ldg(xj + g + c + m * tau), m == 0);
+        }
+        v[c] = (CHECK && !in_range(g + c, lo, hi)) ? never_value<double>() : acc;
+    }
+}
+
+// Diagonal walker: cells (xs[c], xsd[c]) for c = g .. g+kGroup, both operands
+// read from memory; with CHECK, cells at c >= rem are never recurrent.
+template <int NORM, int EMB, bool CHECK>
+__device__ __forceinline__ void diag_group(f2 (&v)[kGroup / 2], const float *__restrict__ xs,
+                                           const float *__restrict__ xsd, long long tau,
+                                           int emb, int g, long long rem) {
+#pragma unroll
+    for (int q = 0; q < kGroup / 2; q++) {
+        const float *ps = xs + g + 2 * q, *pd = xsd + g + 2 * q;
+        Dist2<NORM> d{0.0f, 0.0f};
+        const int ne = EMB > 0 ? EMB : emb;
+#pragma unroll
+        for (int m = 0; m < ne; m++)
+            d.step(pack2(__ldg(ps + m * tau), __ldg(ps + 1 + m * tau)),
+                   pack2(__ldg(pd + m * tau), __ldg(pd + 1 + m * tau)), m == 0);
+        f2 r = d.value();
+        if (CHECK) {
+            const int c = g + 2 * q;
+            r = pack2((long long)c < rem ? lo_of(r) : never_value<float>(),
+                      (long long)c + 1 < rem ? hi_of(r) : never_value<float>());
+        }
+        v[q] = r;
+    }
+}
+template <int NORM, int EMB, bool CHECK>
+__device__ __forceinline__ void diag_group(double (&v)[kGroup], const double *__restrict__ xs,
+                                           const double *__restrict__ xsd, long long tau,
+                                           int emb, int g, long long rem) {
+#pragma unroll
+    for (int c = 0; c < kGroup; c++) {
+        const double acc = cell_dist_mem<double, NORM, EMB>(xs + g + c, xsd + g + c, tau, emb);
+        v[c] = (CHECK && (long long)(g + c) >= rem) ? never_value<double>() : acc;
+    }
+}
+
+// The masks of one 32-cell block of a row (cells xj[0..32)).
+template <typename T, int NORM, int EMB, int NT, bool CHECK>
+__device__ __forceinline__ void row_masks(u32 (&m)[NT], const LaneVec<T, EMB> &a,
+                                          const T *__restrict__ xi, const T *__restrict__ xj,
+                                          long long tau, int emb, long long lo, long long hi,
+                                          const u64 (&keys)[kMaxThrPerPass]) {
+#pragma unroll
+    for (int k = 0; k < NT; k++) m[k] = 0;
+#pragma unroll 1
+    for (int g = 0; g < 32; g += kGroup) {
+        typename GroupOf<T>::type v;
+        row_group<NORM, EMB, CHECK>(v, a, xi, xj, tau, emb, g, lo, hi);
+        push_group<NT>(m, v, keys);
+    }
+}
+
+// The masks of one 32-cell block of a diagonal (cells (xs[c], xsd[c])).
+template <typename T, int NORM, int EMB, int NT, bool CHECK>
+__device__ __forceinline__ void diag_masks(u32 (&m)[NT], const T *__restrict__ xs,
+                                           const T *__restrict__ xsd, long long tau, int emb,
+                                           long long rem, const u64 (&keys)[kMaxThrPerPass]) {
+#pragma unroll
+    for (int k = 0; k < NT; k++) m[k] = 0;
+#pragma unroll 1
+    for (int g = 0; g < 32; g += kGroup) {
+        typename GroupOf<T>::type v;
+        diag_group<NORM, EMB, CHECK>(v, xs, xsd, tau, emb, g, rem);
+        push_group<NT>(m, v, keys);
     }
 }
 
@@ -167,25 +287,14 @@ struct LineSmem {
 // the main-diagonal cell (i, i) is counted once, the others twice.
 // ---------------------------------------------------------------------------
 template <typename T, int NORM, int EMB, int NT, bool CHECK>
-__device__ __forceinline__ void rr_block(const T (&a)[EMB > 0 ? EMB : 1],
+__device__ __forceinline__ void rr_block(const LaneVec<T, EMB> &a,
                                          const T *__restrict__ xi, const T *__restrict__ xj,
                                          long long tau, int emb, long long lo, long long hi,
                                          const u64 (&keys)[kMaxThrPerPass], u32 (&up)[NT]) {
     u32 m[NT];
+    row_masks<T, NORM, EMB, NT, CHECK>(m, a, xi, xj, tau, emb, lo, hi, keys);
 #pragma unroll
-    for (int k = 0; k < NT; k++) m[k] = 0;
-#pragma unroll 1
-    for (int g = 0; g < 32; g += kGroup) {
-        T v[kGroup];
-#pragma unroll
-        for (int c = 0; c < kGroup; c++) {
-            v[c] = cell_dist<T, NORM, EMB>(a, xi, xj + g + c, tau, emb);
-            if (CHECK && !(g + c >= lo && g + c < hi)) v[c] = never_value<T>();
-        }
-        push_group<T, NT>(m, v, keys);
-    }
-#pragma unroll
-    for (int k = 0; k < NT; k++) up[k] += 32u - __popc(m[k]);
+    for (int k = 0; k < NT; k++) up[k] += __popc(m[k]);
 }
 
 template <typename T, int NORM, int EMB, int NT>
@@ -209,14 +318,14 @@ rr_rows(const __grid_constant__ WalkArgs p) {
             if (half == 1 && band == unit) break;
             const long long i = band * 32 + lane;
             const bool row_ok = i < nc;
-            T a[EMB > 0 ? EMB : 1];
-            load_lane_vec<T, EMB>(a, x + i, tau);
+            LaneVec<T, EMB> a;
+            a.load(x + i, tau);
             u32 up[NT], dg[NT];
             {
-                const T v = cell_dist<T, NORM, EMB>(a, x + i, x + i, tau, p.emb);
+                const T v = cell_dist_mem<T, NORM, EMB>(x + i, x + i, tau, p.emb);
 #pragma unroll
                 for (int k = 0; k < NT; k++) {
-                    dg[k] = (row_ok && is_rec(v, p.keys[k])) ? 1u : 0u;
+                    dg[k] = (row_ok && is_rec_lim(v, p.keys[k])) ? 1u : 0u;
                     up[k] = 0;
                 }
             }
@@ -255,18 +364,7 @@ __device__ __forceinline__ void det_block(const T *__restrict__ xs,
                                           const u64 (&keys)[kMaxThrPerPass], const LaneRuns &r,
                                           const Sink &sink) {
     u32 m[NT];
-#pragma unroll
-    for (int k = 0; k < NT; k++) m[k] = 0;
-#pragma unroll 1
-    for (int g = 0; g < 32; g += kGroup) {
-        T v[kGroup];
-#pragma unroll
-        for (int c = 0; c < kGroup; c++) {
-            v[c] = cell_dist_mem<T, NORM, EMB>(xs + g + c, xsd + g + c, tau, emb);
-            if (CHECK && (long long)(g + c) >= rem) v[c] = never_value<T>();
-        }
-        push_group<T, NT>(m, v, keys);
-    }
+    diag_masks<T, NORM, EMB, NT, CHECK>(m, xs, xsd, tau, emb, rem, keys);
     close_block<NT, Sink>(m, r, sink);
 }
 
@@ -317,25 +415,14 @@ det_diags(const __grid_constant__ WalkArgs p) {
 // band striding is balanced.
 // ---------------------------------------------------------------------------
 template <typename T, int NORM, int EMB, int NT, bool CHECK, class Sink>
-__device__ __forceinline__ void lam_block(const T (&a)[EMB > 0 ? EMB : 1],
+__device__ __forceinline__ void lam_block(const LaneVec<T, EMB> &a,
                                           const T *__restrict__ xi,
                                           const T *__restrict__ xj,
                                           long long tau, int emb, long long rem,
                                           const u64 (&keys)[kMaxThrPerPass], const LaneRuns &r,
                                           const Sink &sink) {
     u32 m[NT];
-#pragma unroll
-    for (int k = 0; k < NT; k++) m[k] = 0;
-#pragma unroll 1
-    for (int g = 0; g < 32; g += kGroup) {
-        T v[kGroup];
-#pragma unroll
-        for (int c = 0; c < kGroup; c++) {
-            v[c] = cell_dist<T, NORM, EMB>(a, xi, xj + g + c, tau, emb);
-            if (CHECK && (long long)(g + c) >= rem) v[c] = never_value<T>();
-        }
-        push_group<T, NT>(m, v, keys);
-    }
+    row_masks<T, NORM, EMB, NT, CHECK>(m, a, xi, xj, tau, emb, 0, rem, keys);
     close_block<NT, Sink>(m, r, sink);
 }
 
@@ -360,8 +447,8 @@ lam_rows(const __grid_constant__ WalkArgs p) {
     for (long long band = gwarp; band < p.nbands; band += nwarps) {
         const long long i = band * 32 + lane;
         const bool row_ok = i < nc;
-        T a[EMB > 0 ? EMB : 1];
-        load_lane_vec<T, EMB>(a, x + i, tau);
+        LaneVec<T, EMB> a;
+        a.load(x + i, tau);
         runs_begin<NT>(r);
         long long j0 = 0;
         // All lanes walk together (the group decision is warp-wide); in the

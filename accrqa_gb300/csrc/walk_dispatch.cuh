@@ -67,7 +67,8 @@ static cudaError_t launch_one(const accrqa_walk_desc &d, cudaStream_t st) {
             order[q - 1] = t;
         }
     for (int k = 0; k < kMaxThrPerPass; k++) {
-        a.keys[k] = d.keys[order[k]];
+        a.keys[k] = d.dtype == ACCRQA_F32 ? accrqa_f32_limit_pair(d.keys[order[k]])
+                                          : d.keys[order[k]];
         a.row[k] = order[k] < d.nthr ? order[k] : 0;
     }
     a.counts = (u64 *)d.d_counts;

@@ -276,3 +276,13 @@ def lam_hist_dev(d_hist, stride, d_maxlen, d_x, dtype_code, n, tau, emb, thresho
                  norm, stream=0) -> None:
     _lines_dev("accrqa_gb300_lam_hist_dev", d_hist, stride, d_maxlen, d_x, dtype_code,
                n, tau, emb, thresholds, norm, stream)
+
+
+def probe_fp32(mode: int = 1, reps: int = 20) -> float:
+    """Measured separately rounded multiply/add rate of the current device in
+    operations per second (mode 0 FP32 scalar, 1 packed f32x2, 2 FP64)."""
+    out = ctypes.c_double(0.0)
+    code = _lib.handle().accrqa_gb300_probe_fp32(int(mode), int(reps), ctypes.byref(out))
+    if code:
+        raise EngineError(f"rate probe failed: CUDA error {code}")
+    return float(out.value)

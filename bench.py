@@ -63,6 +63,14 @@ def cells_per_step(measures=3):
     return tot * measures
 
 
+# DRAM bytes (read + write) per launch of the dominant kernel, lam_rows, on
+# this workload, from an ncu capture (dram__bytes_read.sum +
+# dram__bytes_write.sum); None until captured.  The kernel reads the series
+# (0.8 MB, L2-resident) and writes histograms with atomics, so this stays far
+# below what the FP32 side could move.
+LAM_TRAFFIC_PER_LAUNCH = None
+
+
 def algo_ops(nc, emb, nthr):
     """FP32 operations one pass performs by the algorithm's count:
     U * (3*emb + 1 + nthr), U = nc(nc+1)/2 unique pairs (sub, mul, add per
@@ -261,7 +269,12 @@ def run_ours(args):
     dom = max(per_kind, key=lambda k: per_kind[k]["ms"])
     props = torch.cuda.get_device_properties(dev)
     sm_mhz = clk.get("sm_mhz") or 1462.0
-    peak_ops = props.multi_processor_count * 128 * sm_mhz * 1e6   # non-FMA FP32 issue rate
+    derived_ops = props.multi_processor_count * 128 * sm_mhz * 1e6   # 128 FP32 lanes per SM
+    # measured ceiling: separately rounded FP32 multiply/add chains, scalar
+    # and packed f32x2 (the kernels use both); the faster one is the peak
+    probe = {"scalar": engine.probe_fp32(0), "f32x2": engine.probe_fp32(1),
+             "fp64": engine.probe_fp32(2)}
+    peak_ops = max(probe["scalar"], probe["f32x2"])
     achieved = per_kind[dom]["ops"] / (per_kind[dom]["ms"] * 1e-3)
 
     # end to end through the reference-facing API (host buffers)
@@ -313,15 +326,19 @@ def run_ours(args):
         "gpu_launches": int(launches),
         "roofline": {"bound": "fp32", "kernel": dom, "achieved": achieved / 1e12,
                      "peak": peak_ops / 1e12, "unit": "TFLOP/s",
-                     "frac": achieved / peak_ops, "traffic": None,
-                     "peak_source": f"derived: {props.multi_processor_count} SMs x 128 FP32 "
-                                    f"lanes x {sm_mhz:.0f} MHz median SM clock under load",
+                     "frac": achieved / peak_ops, "traffic": LAM_TRAFFIC_PER_LAUNCH,
+                     "peak_source": "measured: multiply/add chain probe "
+                                    "(accrqa_gb300_probe_fp32), best of FP32 scalar and f32x2",
+                     "probe_tflops": {k: v / 1e12 for k, v in probe.items()},
+                     "derived_tflops": derived_ops / 1e12,
                      "ops_per_launch": "U*(3*emb+1+nthr), U=nc(nc+1)/2"},
         "kernels": {k: {"ms_total": v["ms"], "launches": v["launches"],
                         "tflops_algorithmic": v["ops"] / (v["ms"] * 1e-3) / 1e12}
                     for k, v in per_kind.items()},
         "clocks": clk,
     }
+    if rank == 0 and not args.skip_roofline_1m:
+        line["roofline_1m"] = roofline_1m_section(args, peak_ops, probe["fp64"])
     if rank == 0 and not args.skip_batched:
         line["batched"] = batched_section(args)
     if rank == 0 and not args.skip_served:
@@ -580,6 +597,72 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def roofline_1m_section(args, peak_f32, peak_f64):
+    """The N = 1,000,000 roofline workload: white noise and AR(1) (phi 0.95),
+    tau = 1, emb = 5, Euclidean, thresholds {0.1, 0.2, 0.5, 1.0} x std, RR and
+    DET (lmin 2), one device-resident pass each, float32 (and float64 with
+    --roofline-f64).  Reports seconds, cells/s and algorithmic TFLOP/s against
+    the measured multiply/add peak of the pass's dtype."""
+    import torch
+
+    from accrqa_gb300 import engine, workloads
+    n, tau, emb = 1_000_000, 1, 5
+    nc = n - (emb - 1) * tau
+    dev = torch.device("cuda", torch.cuda.current_device())
+    stream = torch.cuda.current_stream(dev)
+    sp = stream.cuda_stream
+    out = []
+    dtypes = [np.float32] + ([np.float64] if args.roofline_f64 else [])
+    for name, gen in (("white", workloads.white), ("ar1", workloads.ar1)):
+        base = gen(n, SEED + 7)
+        base = (base - base.mean()) / base.std()
+        for dt in dtypes:
+            x = base.astype(dt)
+            tdt = torch.float32 if dt == np.float32 else torch.float64
+            code = engine.F32 if dt == np.float32 else engine.F64
+            std = float(np.std(x.astype(np.float64)))
+            thr = (np.array([0.1, 0.2, 0.5, 1.0]) * std).astype(dt)
+            dx = torch.zeros(n + 128, dtype=tdt, device=dev)
+            dx[:n].copy_(torch.from_numpy(x))
+            hist = torch.zeros(len(thr) * (nc + 1), dtype=torch.int64, device=dev)
+            cnt = torch.zeros(len(thr), dtype=torch.int64, device=dev)
+            mx = torch.zeros(len(thr), dtype=torch.int32, device=dev)
+            # warm the same kernels on a short prefix
+            engine.rr_counts_dev(cnt.data_ptr(), dx.data_ptr(), code, 4096, tau, emb, thr, 1, sp)
+            engine.det_hist_dev(hist.data_ptr(), nc + 1, mx.data_ptr(), dx.data_ptr(), code,
+                                4096, tau, emb, thr, 1, sp)
+            for kind in ("rr", "det"):
+                hist.zero_()
+                cnt.zero_()
+                mx.zero_()
+                torch.cuda.synchronize()
+                a = torch.cuda.Event(enable_timing=True)
+                b = torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                if kind == "rr":
+                    engine.rr_counts_dev(cnt.data_ptr(), dx.data_ptr(), code, n, tau, emb, thr,
+                                         1, sp)
+                else:
+                    engine.det_hist_dev(hist.data_ptr(), nc + 1, mx.data_ptr(), dx.data_ptr(),
+                                        code, n, tau, emb, thr, 1, sp)
+                b.record(stream)
+                b.synchronize()
+                sec = a.elapsed_time(b) * 1e-3
+                ops = algo_ops(nc, emb, len(thr))
+                peak = peak_f32 if dt == np.float32 else peak_f64
+                rr_cells = int(cnt.sum().item()) if kind == "rr" else None
+                out.append({"series": name, "dtype": np.dtype(dt).name, "measure": kind,
+                            "seconds": sec, "cells_per_s": nc * nc * len(thr) / sec,
+                            "tflops_algorithmic": ops / sec / 1e12,
+                            "frac_of_measured_peak": ops / sec / peak,
+                            "recurrent_cells": rr_cells})
+                log(f"1M {name} {np.dtype(dt).name} {kind}: {sec:.3f} s")
+            del dx, hist
+    return {"workload": "N=1e6 white and AR(1) phi=0.95, tau 1, emb 5, Euclidean, thresholds "
+                        "{0.1,0.2,0.5,1.0} x std, RR and DET(lmin 2), one pass each",
+            "ops_per_pass": "U*(3*emb+1+nthr), U=nc(nc+1)/2", "passes": out}
+
+
 def run_case(args):
     """One pass of one kernel on a smaller series (for profiler captures):
     --case rr|det|lam, --n samples, tau=1, emb=5, 16 thresholds."""
@@ -627,6 +710,9 @@ def main(argv=None):
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--skip-batched", action="store_true")
+    ap.add_argument("--skip-roofline-1m", action="store_true")
+    ap.add_argument("--roofline-f64", action="store_true",
+                    help="also run the float64 passes of the N=1e6 roofline workload")
     ap.add_argument("--batch-series", type=int, default=512)
     ap.add_argument("--skip-served", action="store_true")
     ap.add_argument("--serve-rates", type=lambda s: [float(v) for v in s.split(",")], default=[20.0, 60.0])

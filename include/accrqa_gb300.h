@@ -345,6 +345,14 @@ Accrqa_Error accrqa_gb300_rr_dev_noalloc(void *d_rr, const void *d_x, int32_t dt
                                          const void *thresholds, int32_t nthr,
                                          int32_t norm, void *stream);
 
+/* Diagnostics (no counterpart in the reference): the measured rate of
+ * separately rounded multiply and add instructions on the current device, in
+ * operations per second -- the ceiling the walk kernels are held against.
+ * mode 0 = FP32 scalar, 1 = packed f32x2 (two operations each), 2 = FP64.
+ * `reps` timed launches of about a millisecond each.  Returns 0 or a
+ * cudaError_t value. */
+int accrqa_gb300_probe_fp32(int32_t mode, int32_t reps, double *ops_per_s);
+
 #ifdef __cplusplus
 }
 #endif

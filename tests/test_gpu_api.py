@@ -163,3 +163,44 @@ def test_full_size_count_consistency(gpu, n, tau, emb):
     np.testing.assert_array_equal((det * lengths).sum(axis=1), rr)
     nc = n - (emb - 1) * tau
     assert (det[:, nc] == 1).all()
+
+
+def _rr_target_one_step_per_call(x, tau, emb, target, D, epsilon, max_iter, tmin, tmax):
+    """The reference's RR_target loop (src/accrqa/accrqa.py:555-594), one RR
+    call per bisection step."""
+    t_ = np.array([tau], np.intc)
+    e_ = np.array([emb], np.intc)
+
+    def rr(ts):
+        return A.RR(x, t_, e_, np.array(ts, np.float32).astype(x.dtype), D,
+                    tidy_data=False).flatten()
+
+    mid = (tmax - tmin) / 2.0 + tmin
+    v = rr([tmin, mid, tmax])
+    low, hgh, cur = v[0], v[2], v[1]
+    for _ in range(1, max_iter + 1):
+        mid = (tmax - tmin) / 2.0 + tmin
+        cur = rr([mid])[0]
+        if abs(cur - target) < epsilon or (hgh - low) < epsilon:
+            return mid, cur
+        if cur < target:
+            tmin = mid
+        else:
+            tmax = mid
+    return (tmax - tmin) / 2.0 + tmin, cur
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_rr_target_equals_one_step_per_call(gpu, dt):
+    x = workloads.lorenz_x(3000, 5).astype(dt)
+    x = (x / np.std(x.astype(np.float64))).astype(dt)
+    D = A.accrqaDistance("euclidean")
+    for target, eps, max_iter, tmin, tmax in [(0.05, 0.01, 20, 0.0, 10.0),
+                                             (0.05, 1e-6, 20, 0.0, 10.0),
+                                             (0.2, 1e-4, 7, 0.0, 5.0),
+                                             (0.01, 1e-9, 30, 0.0, 10.0),
+                                             (0.5, 1e-3, 3, 0.1, 4.0)]:
+        got = A.RR_target(x, 2, 3, target, D, epsilon=eps, max_iter=max_iter,
+                          threshold_min=tmin, threshold_max=tmax)
+        want = _rr_target_one_step_per_call(x, 2, 3, target, D, eps, max_iter, tmin, tmax)
+        assert got[0] == want[0] and got[1] == want[1], (target, eps, got, want)

@@ -54,6 +54,19 @@ def test_threshold_pass_splitting(gpu, oracle_mod, nthr):
         np.testing.assert_array_equal(det[k], oracle_mod.det_hist(x, 2, 3, t, 1))
 
 
+def _nan_variety(dt):
+    if dt == np.float32:
+        bits = np.array([0xFFC00000, 0x7FC00001, 0xFF800001, 0x7F800001], np.uint32)
+    else:
+        bits = np.array([0xFFF8000000000000, 0x7FF8000000000001, 0xFFF0000000000001,
+                         0x7FF0000000000001], np.uint64)
+    big = np.finfo(dt).max
+    nans = bits.view(dt)
+    base = np.array([0.1, 0.2, 0.15, big, -big, 0.12, 0.11, 0.3, 1e30, -1e30, 0.1, 0.2], dt)
+    # concatenation keeps every NaN's bits as they are
+    return np.concatenate([np.concatenate([base, nans[k % 4:k % 4 + 1]]) for k in range(8)])
+
+
 @pytest.mark.parametrize("dt", [np.float32, np.float64])
 def test_edge_series(gpu, oracle_mod, dt):
     specials = {
@@ -63,6 +76,9 @@ def test_edge_series(gpu, oracle_mod, dt):
         "nan_inf": np.array([0.1, np.nan, 0.3, np.inf, 0.2, -np.inf, 0.25, 0.26, 0.27,
                              0.1, 0.3, 0.5] * 4),
         "long_lines": np.tile(np.arange(10) / 10.0, 70),   # periodic: lines of length ~nc
+        # NaNs of both signs and with payloads, and values whose squared
+        # differences overflow to inf
+        "nan_signs": _nan_variety(dt),
     }
     thr = np.array([-1.0, -0.0, 0.0, 0.05, 0.1, 0.5, np.inf, np.nan], dtype=dt)
     for name, s in specials.items():

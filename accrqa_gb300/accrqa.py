@@ -344,12 +344,3 @@ def RR_target(input_data, tau: int, emb: int, target_RR: float, distance_type,
     print(f"Warning: Bisection search stopped after {max_iter} iterations")
     mid = (threshold_max - threshold_min) / 2.0 + threshold_min
     return mid, current_RR
-        if (hgh_RR - low_RR) < epsilon:
-            return mid, current_RR
-        if current_RR < target_RR:
-            threshold_min = mid
-        else:
-            threshold_max = mid
-    print(f"Warning: Bisection search stopped after {max_iter} iterations")
-    mid = (threshold_max - threshold_min) / 2.0 + threshold_min
-    return mid, current_RR

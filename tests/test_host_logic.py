@@ -238,3 +238,47 @@ def test_output_sizes(lib):
     f.restype = ctypes.c_int64
     f.argtypes = [ctypes.c_int64] * 3
     assert f(100, 2, 3) == 96
+
+
+def _fake_rr(calls):
+    """A monotone stand-in for the RR call (float32 thresholds in, rates out)."""
+    def rr(x, taus, embs, thr, D, comp_platform=None, tidy_data=True):
+        calls.append(len(thr))
+        t = np.asarray(thr, np.float64)
+        return np.clip(np.sqrt(t) / 2.5, 0.0, 1.0).reshape(1, 1, -1)
+    return rr
+
+
+@pytest.mark.parametrize("target,eps,max_iter,tmin,tmax", [
+    (0.3, 0.01, 20, 0.0, 10.0), (0.3, 1e-9, 20, 0.0, 10.0), (0.71, 1e-7, 7, 0.0, 5.0),
+    (0.05, 1e-12, 30, 0.0, 10.0), (0.5, 1e-3, 3, 0.1, 4.0), (0.9, 0.5, 5, 0.0, 1.0)])
+def test_rr_target_tree_walk_equals_bisection(monkeypatch, target, eps, max_iter, tmin, tmax):
+    import accrqa_gb300 as A
+    from accrqa_gb300 import accrqa as mod
+    calls = []
+    monkeypatch.setattr(mod, "RR", _fake_rr(calls))
+    x = np.zeros(100, np.float32)
+    D = A.accrqaDistance("euclidean")
+    got = A.RR_target(x, 1, 2, target, D, epsilon=eps, max_iter=max_iter,
+                      threshold_min=tmin, threshold_max=tmax)
+    # the reference's loop, one midpoint per call
+    rr = _fake_rr([])
+    lo, hi = tmin, tmax
+    mid = (hi - lo) / 2.0 + lo
+    v = rr(x, 0, 0, np.array([lo, mid, hi], np.float32), D).flatten()
+    low, hgh, cur = v[0], v[2], v[1]
+    want = None
+    for _ in range(1, max_iter + 1):
+        mid = (hi - lo) / 2.0 + lo
+        cur = rr(x, 0, 0, np.array([mid], np.float32), D).flatten()[0]
+        if abs(cur - target) < eps or (hgh - low) < eps:
+            want = (mid, cur)
+            break
+        if cur < target:
+            lo = mid
+        else:
+            hi = mid
+    if want is None:
+        want = ((hi - lo) / 2.0 + lo, cur)
+    assert got[0] == want[0] and got[1] == want[1]
+    assert len(calls) <= 1 + -(-max_iter // 4)   # the first call, then one per 4 steps

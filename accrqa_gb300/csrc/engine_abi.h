@@ -17,7 +17,11 @@ enum accrqa_walk_kind {
     ACCRQA_WALK_LAM = 2   /* row-run histograms of the full matrix */
 };
 
-enum accrqa_dtype { ACCRQA_F32 = 0, ACCRQA_F64 = 1 };
+enum accrqa_dtype {
+    ACCRQA_F32 = 0,
+    ACCRQA_F64 = 1,
+    ACCRQA_F64F = 2   /* float64 decided through the float filter (batched launches) */
+};
 
 #define ACCRQA_MAX_THR_PER_PASS 16
 #define ACCRQA_SERIES_PAD 128
@@ -50,6 +54,14 @@ typedef struct accrqa_walk_desc {
     uint64_t *d_hist;        /* DET/LAM: [nthr][hist_stride] (zero first) */
     int64_t hist_stride;     /* >= nc + 1 */
     uint32_t *d_maxlen;      /* DET/LAM: [nthr] longest line >= ACCRQA_SHORT_RUN_BINS */
+    /* float64 only, optional: the series split into float hi = RN(x) and
+     * lo = RN(x - hi) (each >= n + ACCRQA_SERIES_PAD elements) and the float
+     * filter's limit pairs per threshold (accrqa_f64_filter_pair); when
+     * d_xhi is set the pass decides cells in float and only the ambiguous
+     * ones in double -- same results, float speed. */
+    const void *d_xhi;
+    const void *d_xlo;
+    uint64_t filter_keys[ACCRQA_MAX_THR_PER_PASS];
 } accrqa_walk_desc;
 
 /* Enqueue one pass on `stream` (a cudaStream_t, 0 = legacy default stream).
@@ -72,7 +84,8 @@ uint64_t accrqa_gb300_launch_count(void);
 /* ---- batched passes (many series per launch) ---------------------------- */
 
 /* One series' pass as the batched kernels read it (device memory).  Keys are
- * in kernel form (float: accrqa_f32_limit_pair) and sorted by decreasing
+ * in kernel form (float: accrqa_f32_limit_pair; filtered float64: the filter
+ * pairs) and sorted by decreasing
  * threshold, row[k] is the output row of slot k, padding
  * slots hold the never-recurrent key.  Same layout as accrqa::BatchJob. */
 typedef struct accrqa_batch_job {
@@ -89,6 +102,11 @@ typedef struct accrqa_batch_job {
     uint64_t *hist;
     int64_t hist_stride;
     uint32_t *maxlen;
+    /* float-filtered float64 jobs: hi/lo split of the series; keys[] hold the
+     * filter pairs and xkeys[] the exact limits */
+    const float *xhi;
+    const float *xlo;
+    uint64_t xkeys[ACCRQA_MAX_THR_PER_PASS];
 } accrqa_batch_job;
 
 typedef struct accrqa_batch_unit {

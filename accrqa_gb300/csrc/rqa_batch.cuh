@@ -28,8 +28,8 @@ struct BatchUnit {
 
 template <int NT>
 struct BatchSmem {
-    // per warp: bins [NT][kBatchBins], longest run [kMaxThrPerPass], run state 2*NT*32
-    static constexpr int kWarpWords = NT * kBatchBins + kMaxThrPerPass + 2 * NT * 32;
+    // per warp: bins [NT][kBatchBins], longest run [kMaxThrPerPass]
+    static constexpr int kWarpWords = NT * kBatchBins + kMaxThrPerPass;
     static constexpr size_t kBytes = (size_t)kWarpsPerCta * kWarpWords * sizeof(u32);
 };
 
@@ -52,6 +52,15 @@ __device__ __forceinline__ void batch_flush(u32 *bins, u32 *bmax, const BatchJob
     __syncwarp();
 }
 
+template <typename T>
+__device__ __forceinline__ typename SeriesOf<T>::ptr batch_series(const BatchJob &j) {
+    return (const T *)j.x;
+}
+template <>
+__device__ __forceinline__ F64FPtr batch_series<F64F>(const BatchJob &j) {
+    return F64FPtr{(const double *)j.x, j.xhi, j.xlo};
+}
+
 // Sink whose short bins are the warp's own.
 struct WarpSink {
     u32 *sh;
@@ -67,6 +76,10 @@ struct WarpSink {
             atomicMax(&shmax[k], len);
         }
     }
+    // A run inside one block is shorter than 32: always a shared bin.
+    __device__ __forceinline__ void emit_short(int k, u32 len) const {
+        atomicAdd(&sh[k * kBatchBins + len], 1u);
+    }
 };
 
 template <int KIND, typename T, int NORM, int EMB, int NT>
@@ -78,8 +91,7 @@ batch_walk(const BatchJob *__restrict__ jobs, const BatchUnit *__restrict__ unit
     u32 *wbase = smem + warp * BatchSmem<NT>::kWarpWords;
     u32 *bins = wbase;
     u32 *bmax = bins + NT * kBatchBins;
-    u32 *runs = bmax + kMaxThrPerPass;
-    const LaneRuns r{runs, runs + NT * 32, lane};
+    u32 carry[NT];
     for (int t = lane; t < NT * kBatchBins; t += 32) bins[t] = 0;
     if (lane < kMaxThrPerPass) bmax[lane] = 0;
     __syncwarp();
@@ -90,6 +102,7 @@ batch_walk(const BatchJob *__restrict__ jobs, const BatchUnit *__restrict__ unit
 
     int cur = -1;
     u64 keys[kMaxThrPerPass];
+    const u64 *xkeys = nullptr;   // exact limits (the filtered float64 jobs' are apart)
     const BatchJob *jp = nullptr;
     u64 total = 0;   // RR: lane k holds slot k's count for the current series
     for (int u = u_begin; u < u_end; u++) {
@@ -107,8 +120,9 @@ batch_walk(const BatchJob *__restrict__ jobs, const BatchUnit *__restrict__ unit
             jp = jobs + cur;
 #pragma unroll
             for (int k = 0; k < kMaxThrPerPass; k++) keys[k] = jp->keys[k];
+            xkeys = std::is_same<T, F64F>::value ? (const u64 *)jp->xkeys : (const u64 *)jp->keys;
         }
-        const T *__restrict__ x = (const T *)jp->x;
+        const typename SeriesOf<T>::ptr x = batch_series<T>(*jp);
         const long long nc = jp->nc, nbands = jp->nbands;
         const long long tau = jp->tau;
         const int emb = jp->emb;
@@ -119,20 +133,20 @@ batch_walk(const BatchJob *__restrict__ jobs, const BatchUnit *__restrict__ unit
             LaneVec<T, EMB> a;
             a.load(x + i, tau);
             const WarpSink sink{bins, bmax, (u64 *)jp->hist, jp->hist_stride, jp->row};
-            runs_begin<NT>(r);
+            runs_begin<NT>(carry);
             long long j0 = 0;
             if (band * 32 + 31 < nc) {
                 for (; j0 + 32 <= nc; j0 += 32)
-                    lam_block<T, NORM, EMB, NT, false>(a, x + i, x + j0, tau, emb, 32, keys, r, sink);
+                    lam_block<T, NORM, EMB, NT, false>(a, x + i, x + j0, tau, emb, 32, keys, xkeys, carry, sink);
                 if (j0 < nc)
-                    lam_block<T, NORM, EMB, NT, true>(a, x + i, x + j0, tau, emb, nc - j0, keys, r,
+                    lam_block<T, NORM, EMB, NT, true>(a, x + i, x + j0, tau, emb, nc - j0, keys, xkeys, carry,
                                                       sink);
             } else {
                 for (; j0 < nc; j0 += 32)
                     lam_block<T, NORM, EMB, NT, true>(a, x + i, x + j0, tau, emb,
-                                                      row_ok ? nc - j0 : 0, keys, r, sink);
+                                                      row_ok ? nc - j0 : 0, keys, xkeys, carry, sink);
             }
-            runs_end<NT, WarpSink>(r, sink);
+            runs_end<NT, WarpSink>(carry, sink);
         } else {
 #pragma unroll 1
             for (int half = 0; half < 2; half++) {
@@ -144,15 +158,15 @@ batch_walk(const BatchJob *__restrict__ jobs, const BatchUnit *__restrict__ unit
                     const long long len = nc - d;
                     const long long wmin = nc - (band * 32 + 32);
                     const long long wmax = nc - (band * 32 + 1);
-                    runs_begin<NT>(r);
+                    runs_begin<NT>(carry);
                     long long s0 = 0;
                     for (; s0 + 32 <= wmin; s0 += 32)
                         det_block<T, NORM, EMB, NT, false>(x + s0, x + s0 + d, tau, emb, 32, keys,
-                                                           r, sink);
+                                                           xkeys, carry, sink);
                     for (; s0 < wmax; s0 += 32)
                         det_block<T, NORM, EMB, NT, true>(x + s0, x + s0 + d, tau, emb, len - s0,
-                                                          keys, r, sink);
-                    runs_end<NT, WarpSink>(r, sink);
+                                                          keys, xkeys, carry, sink);
+                    runs_end<NT, WarpSink>(carry, sink);
                 } else {
                     const long long i = band * 32 + lane;
                     const bool row_ok = i < nc;
@@ -160,23 +174,25 @@ batch_walk(const BatchJob *__restrict__ jobs, const BatchUnit *__restrict__ unit
                     a.load(x + i, tau);
                     u32 up[NT], dg[NT];
                     {
-                        const T v = cell_dist_mem<T, NORM, EMB>(x + i, x + i, tau, emb);
+                        const auto v = cell_dist_mem<typename SeriesOf<T>::exact, NORM, EMB>(
+                            exact_ptr(x + i), exact_ptr(x + i), tau, emb);
 #pragma unroll
                         for (int k = 0; k < NT; k++) {
-                            dg[k] = (row_ok && is_rec_lim(v, keys[k])) ? 1u : 0u;
+                            dg[k] = (row_ok && is_rec_lim(v, xkeys[k])) ? 1u : 0u;
                             up[k] = 0;
                         }
                     }
                     const long long j0 = band * 32;
                     const long long hi0 = nc - j0 < 32 ? nc - j0 : 32;
                     rr_block<T, NORM, EMB, NT, true>(a, x + i, x + j0, tau, emb, lane + 1, hi0, keys,
-                                                     up);
+                                                     xkeys, up);
                     long long jb = j0 + 32;
                     for (; jb + 32 <= nc; jb += 32)
-                        rr_block<T, NORM, EMB, NT, false>(a, x + i, x + jb, tau, emb, 0, 32, keys, up);
+                        rr_block<T, NORM, EMB, NT, false>(a, x + i, x + jb, tau, emb, 0, 32, keys,
+                                                          xkeys, up);
                     if (jb < nc)
                         rr_block<T, NORM, EMB, NT, true>(a, x + i, x + jb, tau, emb, 0, nc - jb, keys,
-                                                         up);
+                                                         xkeys, up);
 #pragma unroll
                     for (int k = 0; k < NT; k++) {
                         u64 t = 2ull * (u64)(row_ok ? up[k] : 0u) + (u64)dg[k];

@@ -25,6 +25,7 @@
 #pragma once
 
 #include <cstdint>
+#include <type_traits>
 #include <cuda_runtime.h>
 
 namespace accrqa {
@@ -62,6 +63,12 @@ struct WalkArgs {
     u32 *maxlen;            // [nthr] longest line seen
     long long nbands;       // 32-line bands
     long long nunits;       // work units (band pairs)
+    // float64 series through the float filter (F64F kernels only): the
+    // series split into float hi/lo parts, and the exact limits of the slots
+    // (keys[] then hold the filter's float limit pairs)
+    const float *xhi;
+    const float *xlo;
+    u64 xkeys[kMaxThrPerPass];
 };
 
 // ---------------------------------------------------------------------------
@@ -149,6 +156,46 @@ __device__ __forceinline__ f2 add2(f2 a, f2 b) {
     asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
     return r;
 }
+
+// ---------------------------------------------------------------------------
+// float64 series through a float filter.  Every sample x is split into
+// floats hi = RN(x) and lo = RN(x - hi), the distance is evaluated in float
+// from (hi_a - hi_b) + (lo_a - lo_b), and the host turns each exact double
+// limit into two float limits (klo, khi) from a proven error bound of that
+// evaluation: v_f < klo means recurrent, v_f >= khi means not recurrent,
+// and only a cell in between (a band ~1e-6 wide, relative) is evaluated
+// again exactly in double.  The host enables it only for finite series with
+// max|x| <= 2^60 (so that nothing overflows or turns NaN in float).
+// ---------------------------------------------------------------------------
+struct F64F {};
+
+struct F64FPtr {
+    const double *d;   // the series itself (exact fallback)
+    const float *h;    // RN(x)
+    const float *l;    // RN(x - hi)
+    __device__ __forceinline__ F64FPtr operator+(long long o) const { return {d + o, h + o, l + o}; }
+};
+
+// How a kernel instantiation sees its series.
+template <typename T> struct SeriesOf {
+    typedef const T *ptr;
+    typedef T exact;
+};
+template <> struct SeriesOf<F64F> {
+    typedef F64FPtr ptr;
+    typedef double exact;
+};
+template <typename T>
+__device__ __forceinline__ typename SeriesOf<T>::ptr series_ptr(const WalkArgs &p) {
+    return (const T *)p.x;
+}
+template <>
+__device__ __forceinline__ F64FPtr series_ptr<F64F>(const WalkArgs &p) {
+    return F64FPtr{(const double *)p.x, p.xhi, p.xlo};
+}
+template <typename T>
+__device__ __forceinline__ const T *exact_ptr(const T *x) { return x; }
+__device__ __forceinline__ const double *exact_ptr(F64FPtr x) { return x.d; }
 
 // Distances of two cells from their operand pairs a[m], b[m] (m = 0..emb-1).
 // Euclidean: difference and square on the f32x2 pipe, the running sum in the
@@ -248,13 +295,10 @@ __device__ __forceinline__ void push_group(u32 (&m)[NT], const double (&v)[kGrou
     }
 }
 
-// Recurrent-cell mask in walk order (bit c = c-th pushed cell).
-__device__ __forceinline__ u32 walk_mask(u32 m) { return __brev(m); }
-
 // ---------------------------------------------------------------------------
-// Line-length bookkeeping.  A 32-bit mask holds 32 consecutive cells of one
-// line (bit c = c-th cell in walk order); `carry` is the length of the run
-// that reached the end of the previous mask.
+// Line-length bookkeeping.  A block's mask holds 32 consecutive cells of one
+// line, the first cell of the block in bit 31 (the push order); `carry` is
+// the length of the run still open at the end of the previous block.
 // ---------------------------------------------------------------------------
 struct HistSink {
     u32 *sh;          // shared bins [kMaxThrPerPass][kShortRunBins], by slot
@@ -271,35 +315,32 @@ struct HistSink {
             atomicMax(&shmax[k], len);
         }
     }
+    // A run inside one block is shorter than 32: always a shared bin.
+    __device__ __forceinline__ void emit_short(int k, u32 len) const {
+        atomicAdd(&sh[k * kShortRunBins + len], 1u);
+    }
 };
 
-// Close the runs of one mask.  Runs that end inside the mask are emitted,
-// the run touching the top bit is carried.
+// Close slot k's runs of one block for one lane.  The ones at the top of m
+// continue the open run (carry), which ends at the block's first zero; runs
+// strictly inside the block are emitted; the ones at the bottom stay open.
+// Straight-line code apart from the emits, so the lanes of a warp stay
+// together whatever their masks look like.
 template <class Sink>
-__device__ __forceinline__ void runs_of_mask(u32 m, u32 &carry, int k, const Sink &sink) {
-    if (m == 0u) {
-        if (carry) {
-            sink.emit(k, carry);
-            carry = 0;
-        }
-        return;
-    }
-    if (m == 0xFFFFFFFFu) {
-        carry += 32u;
-        return;
-    }
-    u32 lead = (u32)(__ffs(~m) - 1);          // ones at the bottom
-    u32 first = carry + lead;
-    if (first) sink.emit(k, first);
-    u32 hi = (u32)__clz(~m);                  // ones at the top
-    u32 mid = (m & (m + 1u)) & (0xFFFFFFFFu >> hi);
+__device__ __forceinline__ void close_slot(u32 m, u32 &carry, int k, const Sink &sink) {
+    const bool full = m == 0xFFFFFFFFu;
+    const u32 lead = (u32)__clz(~m);                    // ones at the top (32 when full)
+    const u32 first = carry + lead;                     // the open run, if it ends here
+    if (!full && first) sink.emit(k, first);
+    const u32 trail = m & ~(m + 1u);                    // ones at the bottom
+    u32 mid = m & ~trail & __funnelshift_rc(0xFFFFFFFFu, 0u, lead);
+    carry = full ? carry + 32u : (u32)__popc(trail);
     while (mid) {
-        int t = __ffs(mid) - 1;
-        u32 len = (u32)(__ffs(~(mid >> t)) - 1);
-        sink.emit(k, len);
-        mid &= mid + (1u << t);
+        const u32 t = (u32)__clz(mid);                  // start of the next inside run
+        const u32 len = (u32)__clz(~(mid << t));        // its length (< 32)
+        sink.emit_short(k, len);
+        mid &= __funnelshift_rc(0xFFFFFFFFu, 0u, t + len);
     }
-    carry = hi;
 }
 
 }  // namespace accrqa

@@ -32,6 +32,9 @@
 namespace accrqa {
 
 constexpr int kWarpsPerCta = 4;
+// Resident CTAs per SM the line kernels are compiled for (register cap): the
+// diagonal walker waits on loads and needs the warps to hide them.
+constexpr int kLineMinCtas = 6;
 constexpr int kSeriesPad = 128;
 
 // Distance of one cell with both operands read from memory (scalar path:
@@ -78,10 +81,25 @@ struct LaneVec<float, EMB> {
     }
 };
 
-// The values of one group of kGroup cells: float as cell pairs.
+template <int EMB>
+struct LaneVec<F64F, EMB> {
+    f2 h[EMB > 0 ? EMB : 1], l[EMB > 0 ? EMB : 1];
+    __device__ __forceinline__ void load(F64FPtr xi, long long tau) {
+#pragma unroll
+        for (int m = 0; m < EMB; m++) {
+            const float th = __ldg(xi.h + m * tau), tl = __ldg(xi.l + m * tau);
+            h[m] = pack2(th, th);
+            l[m] = pack2(tl, tl);
+        }
+    }
+};
+
+// The values of one group of kGroup cells: float (and the float filter of
+// float64) as cell pairs.
 template <typename T> struct GroupOf;
 template <> struct GroupOf<float> { typedef f2 type[kGroup / 2]; };
 template <> struct GroupOf<double> { typedef double type[kGroup]; };
+template <> struct GroupOf<F64F> { typedef f2 type[kGroup / 2]; };
 
 __device__ __forceinline__ bool in_range(int c, long long lo, long long hi) {
     return (long long)c >= lo && (long long)c < hi;
@@ -173,34 +191,187 @@ __device__ __forceinline__ void diag_group(double (&v)[kGroup], const double *__
     }
 }
 
+// Float filter distance of a cell pair from the hi/lo parts of its operands:
+// d = (a_hi - b_hi) + (a_lo - b_lo) per dimension.  Contraction into fused
+// multiply-adds is harmless here: it only makes the error smaller than the
+// bound the host limits are built from.
+template <int NORM>
+struct DistF2 {
+    f2 acc;
+    float ml, mh;
+    __device__ __forceinline__ void step(f2 ah, f2 al, f2 bh, f2 bl, bool first) {
+        const f2 d = add2(sub2(ah, bh), sub2(al, bl));
+        if (NORM == kNormEuclidean) {
+            const f2 sq = mul2(d, d);
+            acc = first ? sq : add2(acc, sq);
+        } else {
+            ml = fmaxf(first ? 0.0f : ml, fabsf(lo_of(d)));
+            mh = fmaxf(first ? 0.0f : mh, fabsf(hi_of(d)));
+        }
+    }
+    __device__ __forceinline__ f2 value() const {
+        return NORM == kNormEuclidean ? acc : pack2(ml, mh);
+    }
+};
+
+template <int NORM, int EMB, bool CHECK>
+__device__ __forceinline__ void row_group(f2 (&v)[kGroup / 2], const LaneVec<F64F, EMB> &a,
+                                          F64FPtr xi, F64FPtr xj, long long tau, int emb,
+                                          int g, long long lo, long long hi) {
+#pragma unroll
+    for (int q = 0; q < kGroup / 2; q++) {
+        const long long o = g + 2 * q;
+        DistF2<NORM> d{0, 0.0f, 0.0f};
+        const int ne = EMB > 0 ? EMB : emb;
+#pragma unroll
+        for (int m = 0; m < ne; m++) {
+            const long long t = o + m * tau;
+            const f2 bh = pack2(__ldg(xj.h + t), __ldg(xj.h + t + 1));
+            const f2 bl = pack2(__ldg(xj.l + t), __ldg(xj.l + t + 1));
+            if (EMB > 0) {
+                d.step(a.h[EMB > 0 ? m : 0], a.l[EMB > 0 ? m : 0], bh, bl, m == 0);
+            } else {
+                const float th = __ldg(xi.h + m * tau), tl = __ldg(xi.l + m * tau);
+                d.step(pack2(th, th), pack2(tl, tl), bh, bl, m == 0);
+            }
+        }
+        f2 r = d.value();
+        if (CHECK) {
+            const int c = g + 2 * q;
+            r = pack2(in_range(c, lo, hi) ? lo_of(r) : never_value<float>(),
+                      in_range(c + 1, lo, hi) ? hi_of(r) : never_value<float>());
+        }
+        v[q] = r;
+    }
+}
+
+template <int NORM, int EMB, bool CHECK>
+__device__ __forceinline__ void diag_group(f2 (&v)[kGroup / 2], F64FPtr xs, F64FPtr xsd,
+                                           long long tau, int emb, int g, long long rem) {
+#pragma unroll
+    for (int q = 0; q < kGroup / 2; q++) {
+        const long long o = g + 2 * q;
+        DistF2<NORM> d{0, 0.0f, 0.0f};
+        const int ne = EMB > 0 ? EMB : emb;
+#pragma unroll
+        for (int m = 0; m < ne; m++) {
+            const long long t = o + m * tau;
+            d.step(pack2(__ldg(xs.h + t), __ldg(xs.h + t + 1)),
+                   pack2(__ldg(xs.l + t), __ldg(xs.l + t + 1)),
+                   pack2(__ldg(xsd.h + t), __ldg(xsd.h + t + 1)),
+                   pack2(__ldg(xsd.l + t), __ldg(xsd.l + t + 1)), m == 0);
+        }
+        f2 r = d.value();
+        if (CHECK) {
+            const int c = g + 2 * q;
+            r = pack2((long long)c < rem ? lo_of(r) : never_value<float>(),
+                      (long long)c + 1 < rem ? hi_of(r) : never_value<float>());
+        }
+        v[q] = r;
+    }
+}
+
+// Filtered push of one group: keys[k] holds (klo, khi) of slot k.  One f32x2
+// subtraction per cell and slot gives both signs: v < klo (recurrent, pushed
+// into the mask) and v < khi (possibly recurrent); a cell with the two
+// different at some slot is ambiguous.  Returns the ambiguous cells, bit
+// (kGroup-1-c) for cell c (the masks' bit order).
+template <int NT>
+__device__ __forceinline__ u32 push_group_filtered(u32 (&m)[NT], const f2 (&v)[kGroup / 2],
+                                                   const u64 (&keys)[kMaxThrPerPass]) {
+    const float khi0 = __uint_as_float((u32)(keys[0] >> 32));
+    const f2 khi0x2 = pack2(khi0, khi0);
+    u64 any = 0;
+#pragma unroll
+    for (int q = 0; q < kGroup / 2; q++) any |= sub2(v[q], khi0x2);
+    const u32 signs = ((u32)any | (u32)(any >> 32)) >> 31;
+    if (!__any_sync(0xFFFFFFFFu, signs)) {   // every cell surely not recurrent at any slot
+#pragma unroll
+        for (int k = 0; k < NT; k++) m[k] <<= kGroup;
+        return 0u;
+    }
+    u32 amb = 0;
+#pragma unroll
+    for (int c = 0; c < kGroup; c++) {
+        const float vc = (c & 1) ? hi_of(v[c >> 1]) : lo_of(v[c >> 1]);
+        const f2 vv = pack2(vc, vc);
+        u32 diff = 0;
+#pragma unroll
+        for (int k = 0; k < NT; k++) {
+            const f2 d = sub2(vv, keys[k]);
+            m[k] = __funnelshift_l((u32)d, m[k], 1);
+            diff |= (u32)d ^ (u32)(d >> 32);
+        }
+        amb = (amb << 1) | (diff >> 31);
+    }
+    return amb;
+}
+
+// Exact float64 decisions for the ambiguous cells of a group (rare): the
+// reference's distance in double, compared with the exact limits, written
+// over the cell's bit in every slot's mask.  xi/xj point at the cells'
+// operands: cell c of the group is (xi + ci*c, xj + c).
+template <int NORM, int EMB, int NT>
+__device__ __forceinline__ void exact_fixup(u32 (&m)[NT], u32 amb, const double *xi, long long ci,
+                                            const double *xj, long long tau, int emb,
+                                            const u64 *xkeys) {
+#pragma unroll 1
+    for (int c = 0; c < kGroup; c++) {
+        const u32 bit = 1u << (kGroup - 1 - c);
+        if (!__any_sync(0xFFFFFFFFu, (amb & bit) != 0u)) continue;
+        if (amb & bit) {
+            const double v = cell_dist_mem<double, NORM, EMB>(xi + ci * c, xj + c, tau, emb);
+            const u64 b = (u64)__double_as_longlong(v);
+#pragma unroll
+            for (int k = 0; k < NT; k++) m[k] = (m[k] & ~bit) | (b < xkeys[k] ? bit : 0u);
+        }
+    }
+}
+
 // The masks of one 32-cell block of a row (cells xj[0..32)).
 template <typename T, int NORM, int EMB, int NT, bool CHECK>
 __device__ __forceinline__ void row_masks(u32 (&m)[NT], const LaneVec<T, EMB> &a,
-                                          const T *__restrict__ xi, const T *__restrict__ xj,
+                                          typename SeriesOf<T>::ptr xi,
+                                          typename SeriesOf<T>::ptr xj,
                                           long long tau, int emb, long long lo, long long hi,
-                                          const u64 (&keys)[kMaxThrPerPass]) {
+                                          const u64 (&keys)[kMaxThrPerPass], const u64 *xkeys) {
 #pragma unroll
     for (int k = 0; k < NT; k++) m[k] = 0;
 #pragma unroll 1
     for (int g = 0; g < 32; g += kGroup) {
         typename GroupOf<T>::type v;
         row_group<NORM, EMB, CHECK>(v, a, xi, xj, tau, emb, g, lo, hi);
-        push_group<NT>(m, v, keys);
+        if constexpr (std::is_same<T, F64F>::value) {
+            const u32 amb = push_group_filtered<NT>(m, v, keys);
+            if (__any_sync(0xFFFFFFFFu, amb != 0u))
+                exact_fixup<NORM, EMB, NT>(m, amb, exact_ptr(xi), 0, exact_ptr(xj) + g, tau, emb,
+                                           xkeys);
+        } else {
+            push_group<NT>(m, v, keys);
+        }
     }
 }
 
 // The masks of one 32-cell block of a diagonal (cells (xs[c], xsd[c])).
 template <typename T, int NORM, int EMB, int NT, bool CHECK>
-__device__ __forceinline__ void diag_masks(u32 (&m)[NT], const T *__restrict__ xs,
-                                           const T *__restrict__ xsd, long long tau, int emb,
-                                           long long rem, const u64 (&keys)[kMaxThrPerPass]) {
+__device__ __forceinline__ void diag_masks(u32 (&m)[NT], typename SeriesOf<T>::ptr xs,
+                                           typename SeriesOf<T>::ptr xsd, long long tau, int emb,
+                                           long long rem, const u64 (&keys)[kMaxThrPerPass],
+                                           const u64 *xkeys) {
 #pragma unroll
     for (int k = 0; k < NT; k++) m[k] = 0;
 #pragma unroll 1
     for (int g = 0; g < 32; g += kGroup) {
         typename GroupOf<T>::type v;
         diag_group<NORM, EMB, CHECK>(v, xs, xsd, tau, emb, g, rem);
-        push_group<NT>(m, v, keys);
+        if constexpr (std::is_same<T, F64F>::value) {
+            const u32 amb = push_group_filtered<NT>(m, v, keys);
+            if (__any_sync(0xFFFFFFFFu, amb != 0u))
+                exact_fixup<NORM, EMB, NT>(m, amb, exact_ptr(xs) + g, 1, exact_ptr(xsd) + g, tau,
+                                           emb, xkeys);
+        } else {
+            push_group<NT>(m, v, keys);
+        }
     }
 }
 
@@ -225,60 +396,43 @@ __device__ __forceinline__ void hist_smem_flush(const u32 *sh, const u32 *shmax,
         if (shmax[t]) atomicMax(&p.maxlen[p.row[t]], shmax[t]);
 }
 
-// Per-warp run state in shared memory: the 32 lanes' masks and open-run
-// lengths of every slot, [slot][lane].  Keeping them out of registers lets the
-// slot loop below stay a loop (small code, no instruction-cache misses) and
-// stop at the first empty slot.
-struct LaneRuns {
-    u32 *mask;    // [NT][32]
-    u32 *carry;   // [NT][32]
-    int lane;
-    __device__ __forceinline__ u32 &m(int k) const { return mask[k * 32 + lane]; }
-    __device__ __forceinline__ u32 &c(int k) const { return carry[k * 32 + lane]; }
-};
-
+// Open-run lengths of every slot, one lane's line, in registers.
 template <int NT>
-__device__ __forceinline__ void runs_begin(const LaneRuns &r) {
-#pragma unroll 1
-    for (int k = 0; k < NT; k++) r.c(k) = 0;
+__device__ __forceinline__ void runs_begin(u32 (&carry)[NT]) {
+#pragma unroll
+    for (int k = 0; k < NT; k++) carry[k] = 0;
 }
 
 // Close the runs of one 32-cell block for every slot.  Slots nest (slot 0 is
-// the widest threshold): when slot 0 has neither a recurrent cell nor an open
-// run, no slot has one; otherwise slots are visited until the first empty one.
+// the widest threshold): a narrower slot's recurrent cells and open run lie
+// inside the wider slot's, so once no lane of the warp has either at slot k,
+// none has at the narrower slots and the warp stops.
 template <int NT, class Sink>
-__device__ __forceinline__ void close_block(const u32 (&m)[NT], const LaneRuns &r,
+__device__ __forceinline__ void close_block(const u32 (&m)[NT], u32 (&carry)[NT],
                                             const Sink &sink) {
-    if ((walk_mask(m[0]) | r.c(0)) == 0u) return;
 #pragma unroll
-    for (int k = 0; k < NT; k++) r.m(k) = m[k];
-#pragma unroll 1
     for (int k = 0; k < NT; k++) {
-        const u32 rec = walk_mask(r.m(k));
-        u32 carry = r.c(k);
-        if ((rec | carry) == 0u) break;
-        runs_of_mask(rec, carry, k, sink);
-        r.c(k) = carry;
+        if (!__any_sync(0xFFFFFFFFu, (m[k] | carry[k]) != 0u)) return;
+        close_slot(m[k], carry[k], k, sink);
     }
 }
 
-// End of a line: every open run is complete.
+// End of a line: every open run is complete (nested, so the warp stops at
+// the first slot where no lane has one).
 template <int NT, class Sink>
-__device__ __forceinline__ void runs_end(const LaneRuns &r, const Sink &sink) {
-#pragma unroll 1
+__device__ __forceinline__ void runs_end(u32 (&carry)[NT], const Sink &sink) {
+#pragma unroll
     for (int k = 0; k < NT; k++) {
-        const u32 carry = r.c(k);
-        if (carry == 0u) break;   // nested: later slots have shorter runs
-        sink.emit(k, carry);
-        r.c(k) = 0;
+        if (!__any_sync(0xFFFFFFFFu, carry[k] != 0u)) return;
+        if (carry[k]) sink.emit(k, carry[k]);
+        carry[k] = 0;
     }
 }
 
-// Shared memory of the line kernels: histogram bins, longest-run markers and
-// the per-warp run state.
+// Shared memory of the line kernels: histogram bins and longest-run markers.
 template <int NT>
 struct LineSmem {
-    static constexpr int kWords = NT * kShortRunBins + kMaxThrPerPass + 2 * kWarpsPerCta * NT * 32;
+    static constexpr int kWords = NT * kShortRunBins + kMaxThrPerPass;
     static constexpr size_t kBytes = (size_t)kWords * sizeof(u32);
 };
 
@@ -288,11 +442,13 @@ struct LineSmem {
 // ---------------------------------------------------------------------------
 template <typename T, int NORM, int EMB, int NT, bool CHECK>
 __device__ __forceinline__ void rr_block(const LaneVec<T, EMB> &a,
-                                         const T *__restrict__ xi, const T *__restrict__ xj,
+                                         typename SeriesOf<T>::ptr xi,
+                                         typename SeriesOf<T>::ptr xj,
                                          long long tau, int emb, long long lo, long long hi,
-                                         const u64 (&keys)[kMaxThrPerPass], u32 (&up)[NT]) {
+                                         const u64 (&keys)[kMaxThrPerPass], const u64 *xkeys,
+                                         u32 (&up)[NT]) {
     u32 m[NT];
-    row_masks<T, NORM, EMB, NT, CHECK>(m, a, xi, xj, tau, emb, lo, hi, keys);
+    row_masks<T, NORM, EMB, NT, CHECK>(m, a, xi, xj, tau, emb, lo, hi, keys, xkeys);
 #pragma unroll
     for (int k = 0; k < NT; k++) up[k] += __popc(m[k]);
 }
@@ -300,7 +456,9 @@ __device__ __forceinline__ void rr_block(const LaneVec<T, EMB> &a,
 template <typename T, int NORM, int EMB, int NT>
 __global__ void __launch_bounds__(kWarpsPerCta * 32)
 rr_rows(const __grid_constant__ WalkArgs p) {
-    const T *__restrict__ x = (const T *)p.x;
+    const typename SeriesOf<T>::ptr x = series_ptr<T>(p);
+    // exact limits: the float filter of float64 keeps them apart from keys[]
+    const u64 *xkeys = std::is_same<T, F64F>::value ? p.xkeys : p.keys;
     const int lane = threadIdx.x & 31;
     const long long gwarp = (long long)blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);
     const long long nwarps = (long long)gridDim.x * kWarpsPerCta;
@@ -322,23 +480,27 @@ rr_rows(const __grid_constant__ WalkArgs p) {
             a.load(x + i, tau);
             u32 up[NT], dg[NT];
             {
-                const T v = cell_dist_mem<T, NORM, EMB>(x + i, x + i, tau, p.emb);
+                const auto v = cell_dist_mem<typename SeriesOf<T>::exact, NORM, EMB>(
+                    exact_ptr(x + i), exact_ptr(x + i), tau, p.emb);
 #pragma unroll
                 for (int k = 0; k < NT; k++) {
-                    dg[k] = (row_ok && is_rec_lim(v, p.keys[k])) ? 1u : 0u;
+                    dg[k] = (row_ok && is_rec_lim(v, xkeys[k])) ? 1u : 0u;
                     up[k] = 0;
                 }
             }
             // first block: the columns j > i of the diagonal tile (j < nc)
             const long long j0 = band * 32;
             long long hi0 = nc - j0 < 32 ? nc - j0 : 32;
-            rr_block<T, NORM, EMB, NT, true>(a, x + i, x + j0, tau, p.emb, lane + 1, hi0, p.keys, up);
+            rr_block<T, NORM, EMB, NT, true>(a, x + i, x + j0, tau, p.emb, lane + 1, hi0, p.keys,
+                                             xkeys, up);
             // full blocks: j > i for every lane, all columns inside the matrix
             long long jb = j0 + 32;
             for (; jb + 32 <= nc; jb += 32)
-                rr_block<T, NORM, EMB, NT, false>(a, x + i, x + jb, tau, p.emb, 0, 32, p.keys, up);
+                rr_block<T, NORM, EMB, NT, false>(a, x + i, x + jb, tau, p.emb, 0, 32, p.keys, xkeys,
+                                                  up);
             if (jb < nc)
-                rr_block<T, NORM, EMB, NT, true>(a, x + i, x + jb, tau, p.emb, 0, nc - jb, p.keys, up);
+                rr_block<T, NORM, EMB, NT, true>(a, x + i, x + jb, tau, p.emb, 0, nc - jb, p.keys,
+                                                 xkeys, up);
 #pragma unroll
             for (int k = 0; k < NT; k++) {
                 u64 t = 2ull * (u64)(row_ok ? up[k] : 0u) + (u64)dg[k];
@@ -358,29 +520,29 @@ rr_rows(const __grid_constant__ WalkArgs p) {
 // and the line of identity are applied by the host.
 // ---------------------------------------------------------------------------
 template <typename T, int NORM, int EMB, int NT, bool CHECK, class Sink>
-__device__ __forceinline__ void det_block(const T *__restrict__ xs,
-                                          const T *__restrict__ xsd,
+__device__ __forceinline__ void det_block(typename SeriesOf<T>::ptr xs,
+                                          typename SeriesOf<T>::ptr xsd,
                                           long long tau, int emb, long long rem,
-                                          const u64 (&keys)[kMaxThrPerPass], const LaneRuns &r,
-                                          const Sink &sink) {
+                                          const u64 (&keys)[kMaxThrPerPass], const u64 *xkeys,
+                                          u32 (&carry)[NT], const Sink &sink) {
     u32 m[NT];
-    diag_masks<T, NORM, EMB, NT, CHECK>(m, xs, xsd, tau, emb, rem, keys);
-    close_block<NT, Sink>(m, r, sink);
+    diag_masks<T, NORM, EMB, NT, CHECK>(m, xs, xsd, tau, emb, rem, keys, xkeys);
+    close_block<NT, Sink>(m, carry, sink);
 }
 
 template <typename T, int NORM, int EMB, int NT>
-__global__ void __launch_bounds__(kWarpsPerCta * 32)
+__global__ void __launch_bounds__(kWarpsPerCta * 32, kLineMinCtas)
 det_diags(const __grid_constant__ WalkArgs p) {
     extern __shared__ u32 smem[];
     u32 *sh = smem;
     u32 *shmax = smem + NT * kShortRunBins;
-    u32 *runs = shmax + kMaxThrPerPass;
     hist_smem_clear(sh, shmax, NT * kShortRunBins);
     const HistSink sink{sh, shmax, p.hist, p.hist_stride, p.row};
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const LaneRuns r{runs + warp * 2 * NT * 32, runs + warp * 2 * NT * 32 + NT * 32, lane};
+    u32 carry[NT];
 
-    const T *__restrict__ x = (const T *)p.x;
+    const typename SeriesOf<T>::ptr x = series_ptr<T>(p);
+    const u64 *xkeys = std::is_same<T, F64F>::value ? p.xkeys : p.keys;
     const long long gwarp = (long long)blockIdx.x * kWarpsPerCta + warp;
     const long long nwarps = (long long)gridDim.x * kWarpsPerCta;
     const long long nc = p.nc;
@@ -395,15 +557,15 @@ det_diags(const __grid_constant__ WalkArgs p) {
             const long long len = nc - d;                 // cells on this diagonal
             const long long wmin = nc - (band * 32 + 32); // shortest diagonal of the warp
             const long long wmax = nc - (band * 32 + 1);  // longest diagonal of the warp
-            runs_begin<NT>(r);
+            runs_begin<NT>(carry);
             long long s0 = 0;
             for (; s0 + 32 <= wmin; s0 += 32)
-                det_block<T, NORM, EMB, NT, false>(x + s0, x + s0 + d, tau, p.emb, 32, p.keys, r,
-                                                   sink);
+                det_block<T, NORM, EMB, NT, false>(x + s0, x + s0 + d, tau, p.emb, 32, p.keys, xkeys,
+                                                   carry, sink);
             for (; s0 < wmax; s0 += 32)
                 det_block<T, NORM, EMB, NT, true>(x + s0, x + s0 + d, tau, p.emb, len - s0,
-                                                  p.keys, r, sink);
-            runs_end<NT, HistSink>(r, sink);
+                                                  p.keys, xkeys, carry, sink);
+            runs_end<NT, HistSink>(carry, sink);
         }
     }
     hist_smem_flush(sh, shmax, p);
@@ -416,14 +578,14 @@ det_diags(const __grid_constant__ WalkArgs p) {
 // ---------------------------------------------------------------------------
 template <typename T, int NORM, int EMB, int NT, bool CHECK, class Sink>
 __device__ __forceinline__ void lam_block(const LaneVec<T, EMB> &a,
-                                          const T *__restrict__ xi,
-                                          const T *__restrict__ xj,
+                                          typename SeriesOf<T>::ptr xi,
+                                          typename SeriesOf<T>::ptr xj,
                                           long long tau, int emb, long long rem,
-                                          const u64 (&keys)[kMaxThrPerPass], const LaneRuns &r,
-                                          const Sink &sink) {
+                                          const u64 (&keys)[kMaxThrPerPass], const u64 *xkeys,
+                                          u32 (&carry)[NT], const Sink &sink) {
     u32 m[NT];
-    row_masks<T, NORM, EMB, NT, CHECK>(m, a, xi, xj, tau, emb, 0, rem, keys);
-    close_block<NT, Sink>(m, r, sink);
+    row_masks<T, NORM, EMB, NT, CHECK>(m, a, xi, xj, tau, emb, 0, rem, keys, xkeys);
+    close_block<NT, Sink>(m, carry, sink);
 }
 
 template <typename T, int NORM, int EMB, int NT>
@@ -432,13 +594,13 @@ lam_rows(const __grid_constant__ WalkArgs p) {
     extern __shared__ u32 smem[];
     u32 *sh = smem;
     u32 *shmax = smem + NT * kShortRunBins;
-    u32 *runs = shmax + kMaxThrPerPass;
     hist_smem_clear(sh, shmax, NT * kShortRunBins);
     const HistSink sink{sh, shmax, p.hist, p.hist_stride, p.row};
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const LaneRuns r{runs + warp * 2 * NT * 32, runs + warp * 2 * NT * 32 + NT * 32, lane};
+    u32 carry[NT];
 
-    const T *__restrict__ x = (const T *)p.x;
+    const typename SeriesOf<T>::ptr x = series_ptr<T>(p);
+    const u64 *xkeys = std::is_same<T, F64F>::value ? p.xkeys : p.keys;
     const long long gwarp = (long long)blockIdx.x * kWarpsPerCta + warp;
     const long long nwarps = (long long)gridDim.x * kWarpsPerCta;
     const long long nc = p.nc;
@@ -449,22 +611,22 @@ lam_rows(const __grid_constant__ WalkArgs p) {
         const bool row_ok = i < nc;
         LaneVec<T, EMB> a;
         a.load(x + i, tau);
-        runs_begin<NT>(r);
+        runs_begin<NT>(carry);
         long long j0 = 0;
         // All lanes walk together (the group decision is warp-wide); in the
         // last, partial band the rows past nc see only never-recurrent cells.
         if (band * 32 + 31 < nc) {
             for (; j0 + 32 <= nc; j0 += 32)
-                lam_block<T, NORM, EMB, NT, false>(a, x + i, x + j0, tau, p.emb, 32, p.keys, r, sink);
+                lam_block<T, NORM, EMB, NT, false>(a, x + i, x + j0, tau, p.emb, 32, p.keys, xkeys, carry, sink);
             if (j0 < nc)
-                lam_block<T, NORM, EMB, NT, true>(a, x + i, x + j0, tau, p.emb, nc - j0, p.keys, r,
+                lam_block<T, NORM, EMB, NT, true>(a, x + i, x + j0, tau, p.emb, nc - j0, p.keys, xkeys, carry,
                                                   sink);
         } else {
             for (; j0 < nc; j0 += 32)
                 lam_block<T, NORM, EMB, NT, true>(a, x + i, x + j0, tau, p.emb,
-                                                  row_ok ? nc - j0 : 0, p.keys, r, sink);
+                                                  row_ok ? nc - j0 : 0, p.keys, xkeys, carry, sink);
         }
-        runs_end<NT, HistSink>(r, sink);
+        runs_end<NT, HistSink>(carry, sink);
     }
     hist_smem_flush(sh, shmax, p);
 }

@@ -1,6 +1,7 @@
 // batch_dispatch.cuh -- instantiation and launch of the batched kernels.
-// float series get emb-specialised kernels for emb 2..8 (other emb use the
-// generic one); double series use the generic kernel.  Threshold slots are
+// float series and float-filtered double series get emb-specialised kernels
+// for emb 2..8 (other emb use the generic one); unfiltered double series use
+// the generic kernel.  Threshold slots are
 // 8 or 16.
 #pragma once
 
@@ -48,25 +49,28 @@ static cudaError_t batch_nt(const accrqa_batch_launch &L, cudaStream_t st, int *
     return batch_one<KIND, T, NORM, EMB, 16>(L, st, w);
 }
 
-template <int KIND, int NORM>
-static cudaError_t batch_emb_f32(const accrqa_batch_launch &L, cudaStream_t st, int *w) {
+template <int KIND, typename T, int NORM>
+static cudaError_t batch_emb(const accrqa_batch_launch &L, cudaStream_t st, int *w) {
     switch (L.emb) {
-        case 2: return batch_nt<KIND, float, NORM, 2>(L, st, w);
-        case 3: return batch_nt<KIND, float, NORM, 3>(L, st, w);
-        case 4: return batch_nt<KIND, float, NORM, 4>(L, st, w);
-        case 5: return batch_nt<KIND, float, NORM, 5>(L, st, w);
-        case 6: return batch_nt<KIND, float, NORM, 6>(L, st, w);
-        case 7: return batch_nt<KIND, float, NORM, 7>(L, st, w);
-        case 8: return batch_nt<KIND, float, NORM, 8>(L, st, w);
-        default: return batch_nt<KIND, float, NORM, 0>(L, st, w);
+        case 2: return batch_nt<KIND, T, NORM, 2>(L, st, w);
+        case 3: return batch_nt<KIND, T, NORM, 3>(L, st, w);
+        case 4: return batch_nt<KIND, T, NORM, 4>(L, st, w);
+        case 5: return batch_nt<KIND, T, NORM, 5>(L, st, w);
+        case 6: return batch_nt<KIND, T, NORM, 6>(L, st, w);
+        case 7: return batch_nt<KIND, T, NORM, 7>(L, st, w);
+        case 8: return batch_nt<KIND, T, NORM, 8>(L, st, w);
+        default: return batch_nt<KIND, T, NORM, 0>(L, st, w);
     }
 }
 
 template <int KIND>
 static cudaError_t batch_kind(const accrqa_batch_launch &L, cudaStream_t st, int *w) {
     if (L.dtype == ACCRQA_F32) {
-        if (L.norm == kNormEuclidean) return batch_emb_f32<KIND, kNormEuclidean>(L, st, w);
-        if (L.norm == kNormMaximal) return batch_emb_f32<KIND, kNormMaximal>(L, st, w);
+        if (L.norm == kNormEuclidean) return batch_emb<KIND, float, kNormEuclidean>(L, st, w);
+        if (L.norm == kNormMaximal) return batch_emb<KIND, float, kNormMaximal>(L, st, w);
+    } else if (L.dtype == ACCRQA_F64F) {
+        if (L.norm == kNormEuclidean) return batch_emb<KIND, F64F, kNormEuclidean>(L, st, w);
+        if (L.norm == kNormMaximal) return batch_emb<KIND, F64F, kNormMaximal>(L, st, w);
     } else if (L.dtype == ACCRQA_F64) {
         if (L.norm == kNormEuclidean) return batch_nt<KIND, double, kNormEuclidean, 0>(L, st, w);
         if (L.norm == kNormMaximal) return batch_nt<KIND, double, kNormMaximal, 0>(L, st, w);

@@ -240,9 +240,84 @@ static const uint64_t kNeverF64 = 0ull;
 // ===========================================================================
 // Pass planning
 // ===========================================================================
+// ---- float64 filter ----------------------------------------------------------
+bool f64_split(const double *x, int64_t n, float *hi, float *lo, double *maxabs) {
+    double m = 0.0;
+    for (int64_t i = 0; i < n; i++) {
+        const double a = std::fabs(x[i]);
+        if (!(a <= 0x1p60)) return false;   // NaN, inf or too large for float squares
+        if (a > m) m = a;
+        const float h = (float)x[i];
+        hi[i] = h;
+        lo[i] = (float)(x[i] - (double)h);  // x - hi is exact in double
+    }
+    *maxabs = m;
+    return true;
+}
+
+bool f64_filterable(const double *x, int64_t n, double *maxabs) {
+    double m = 0.0;
+    for (int64_t i = 0; i < n; i++) {
+        const double a = std::fabs(x[i]);
+        if (!(a <= 0x1p60)) return false;
+        if (a > m) m = a;
+    }
+    *maxabs = m;
+    return true;
+}
+
+static float round_down_f(double x) {
+    float f = (float)x;
+    if ((double)f > x) f = std::nextafter(f, -INFINITY);
+    return f;
+}
+static float round_up_f(double x) {
+    float f = (float)x;
+    if ((double)f < x) f = std::nextafter(f, INFINITY);
+    return f;
+}
+
+// Error bound of the float evaluation (u = 2^-24, M = max|x|), for every
+// cell: |v_f - v| <= R v + A, v the reference's float64 value.
+//   Each sample: |lo - (x - hi)| <= u^2 |x|.  Per dimension the float
+//   difference d = (hi_a - hi_b) + (lo_a - lo_b) satisfies
+//   |d - delta| <= 2.01 u |delta| + 6.01 u^2 M + 2^-149 (delta = a - b).
+//   Euclidean: squaring adds u, the emb-term sum (emb-1) u, and the cross
+//   terms 2 |delta| (6.01 u^2 M) over emb dimensions give the absolute part:
+//   R = (emb + 4.2) u, A = 24.2 emb u^2 M^2 + O(emb M 2^-149); the float64
+//   reference itself is within (emb + 1) 2^-53 v of the exact sum.
+//   Maximal: |max|d| - max|delta|| <= max |d - delta|: R = 2.1 u,
+//   A = 6.01 u^2 M + 2^-149.
+// The limits below use R = (emb + 5) u / 3 u and A with extra margin, and
+// widen both by 2% more.
+uint64_t f64_filter_pair(uint64_t exact_limit, int norm, int emb, double maxabs) {
+    const double u = 0x1p-24, M = maxabs;
+    double R, A;
+    if (norm == DST_EUCLIDEAN) {
+        R = (emb + 5.0) * u;
+        A = 30.0 * emb * u * u * M * M + 8.0 * emb * (M + 1.0) * 0x1p-149;
+    } else {
+        R = 3.0 * u;
+        A = 10.0 * u * u * M + 0x1p-140;
+    }
+    float klo = -INFINITY, khi = -INFINITY;   // nothing passes: surely not recurrent
+    if (exact_limit != 0) {
+        const uint64_t kb = exact_limit - 1;
+        double key;
+        std::memcpy(&key, &kb, 8);
+        klo = round_down_f(key * (1.0 - 1.02 * R) - 1.02 * A);
+        khi = std::nextafter(round_up_f(key * (1.0 + 1.02 * R) + 1.02 * A), INFINITY);
+    }
+    uint32_t lb, hb;
+    std::memcpy(&lb, &klo, 4);
+    std::memcpy(&hb, &khi, 4);
+    return ((uint64_t)hb << 32) | (uint64_t)lb;
+}
+
 template <typename T>
 static void fill_desc(accrqa_walk_desc &d, int kind, const T *d_x, int64_t n,
-                      int tau, int emb, const T *thr, int k0, int cnt, int norm) {
+                      int tau, int emb, const T *thr, int k0, int cnt, int norm,
+                      const float *d_hi, const float *d_lo, double maxabs) {
     std::memset(&d, 0, sizeof(d));
     d.kind = kind;
     d.dtype = DType<T>::code;
@@ -255,15 +330,22 @@ static void fill_desc(accrqa_walk_desc &d, int kind, const T *d_x, int64_t n,
     const uint64_t never = DType<T>::code == ACCRQA_F32 ? kNeverF32 : kNeverF64;
     for (int k = 0; k < ACCRQA_MAX_THR_PER_PASS; k++)
         d.keys[k] = k < cnt ? threshold_key<T>(thr[k0 + k], norm) : never;
+    if (DType<T>::code == ACCRQA_F64 && d_hi && d_lo) {
+        d.d_xhi = d_hi;
+        d.d_xlo = d_lo;
+        for (int k = 0; k < ACCRQA_MAX_THR_PER_PASS; k++)
+            d.filter_keys[k] = f64_filter_pair(d.keys[k], norm, emb, maxabs);
+    }
 }
 
 template <typename T>
 Accrqa_Error enqueue_rr(const T *d_x, int64_t n, int tau, int emb, const T *thr,
-                        int nthr, int norm, uint64_t *d_counts, cudaStream_t st) {
+                        int nthr, int norm, uint64_t *d_counts, cudaStream_t st,
+                        const float *d_hi, const float *d_lo, double maxabs) {
     for (int k0 = 0; k0 < nthr; k0 += ACCRQA_MAX_THR_PER_PASS) {
         int cnt = nthr - k0 < ACCRQA_MAX_THR_PER_PASS ? nthr - k0 : ACCRQA_MAX_THR_PER_PASS;
         accrqa_walk_desc d;
-        fill_desc<T>(d, ACCRQA_WALK_RR, d_x, n, tau, emb, thr, k0, cnt, norm);
+        fill_desc<T>(d, ACCRQA_WALK_RR, d_x, n, tau, emb, thr, k0, cnt, norm, d_hi, d_lo, maxabs);
         d.d_counts = d_counts + k0;
         int e = accrqa_gb300_launch_walk(&d, st);
         if (e) return cuda_error((cudaError_t)e, "RR kernel launch");
@@ -274,11 +356,12 @@ Accrqa_Error enqueue_rr(const T *d_x, int64_t n, int tau, int emb, const T *thr,
 template <typename T>
 Accrqa_Error enqueue_lines(int kind, const T *d_x, int64_t n, int tau, int emb,
                            const T *thr, int nthr, int norm, uint64_t *d_hist,
-                           int64_t stride, uint32_t *d_maxlen, cudaStream_t st) {
+                           int64_t stride, uint32_t *d_maxlen, cudaStream_t st,
+                           const float *d_hi, const float *d_lo, double maxabs) {
     for (int k0 = 0; k0 < nthr; k0 += ACCRQA_MAX_THR_PER_PASS) {
         int cnt = nthr - k0 < ACCRQA_MAX_THR_PER_PASS ? nthr - k0 : ACCRQA_MAX_THR_PER_PASS;
         accrqa_walk_desc d;
-        fill_desc<T>(d, kind, d_x, n, tau, emb, thr, k0, cnt, norm);
+        fill_desc<T>(d, kind, d_x, n, tau, emb, thr, k0, cnt, norm, d_hi, d_lo, maxabs);
         d.d_hist = d_hist + (int64_t)k0 * stride;
         d.hist_stride = stride;
         d.d_maxlen = d_maxlen + k0;
@@ -288,10 +371,10 @@ Accrqa_Error enqueue_lines(int kind, const T *d_x, int64_t n, int tau, int emb,
     return SUCCESS;
 }
 
-template Accrqa_Error enqueue_rr<float>(const float *, int64_t, int, int, const float *, int, int, uint64_t *, cudaStream_t);
-template Accrqa_Error enqueue_rr<double>(const double *, int64_t, int, int, const double *, int, int, uint64_t *, cudaStream_t);
-template Accrqa_Error enqueue_lines<float>(int, const float *, int64_t, int, int, const float *, int, int, uint64_t *, int64_t, uint32_t *, cudaStream_t);
-template Accrqa_Error enqueue_lines<double>(int, const double *, int64_t, int, int, const double *, int, int, uint64_t *, int64_t, uint32_t *, cudaStream_t);
+template Accrqa_Error enqueue_rr<float>(const float *, int64_t, int, int, const float *, int, int, uint64_t *, cudaStream_t, const float *, const float *, double);
+template Accrqa_Error enqueue_rr<double>(const double *, int64_t, int, int, const double *, int, int, uint64_t *, cudaStream_t, const float *, const float *, double);
+template Accrqa_Error enqueue_lines<float>(int, const float *, int64_t, int, int, const float *, int, int, uint64_t *, int64_t, uint32_t *, cudaStream_t, const float *, const float *, double);
+template Accrqa_Error enqueue_lines<double>(int, const double *, int64_t, int, int, const double *, int, int, uint64_t *, int64_t, uint32_t *, cudaStream_t, const float *, const float *, double);
 
 // ===========================================================================
 // Histogram post-processing
@@ -413,15 +496,46 @@ double LineHistogram::rr() const {
 // ===========================================================================
 // Shared helpers for the drivers
 // ===========================================================================
+// The series on the device as the passes read it.
 template <typename T>
-static Accrqa_Error upload_series(Context &c, const T *x, int64_t n, const T **d_x) {
+struct DevSeries {
+    const T *x = nullptr;
+    const float *hi = nullptr, *lo = nullptr;   // float64: the filter's split
+    double maxabs = 0.0;
+};
+
+template <typename T>
+static Accrqa_Error upload_series(Context &c, const T *x, int64_t n, DevSeries<T> *out) {
     const size_t bytes = (size_t)(n + ACCRQA_SERIES_PAD) * sizeof(T);
     CU(c.series.reserve(bytes), "cudaMalloc(series)");
     CU(copy_async(c.series.ptr, x, (size_t)n * sizeof(T), cudaMemcpyHostToDevice,
                        c.stream), "cudaMemcpy(series H2D)");
     CU(cudaMemsetAsync((T *)c.series.ptr + n, 0, ACCRQA_SERIES_PAD * sizeof(T), c.stream),
        "cudaMemset(series pad)");
-    *d_x = (const T *)c.series.ptr;
+    *out = DevSeries<T>();
+    out->x = (const T *)c.series.ptr;
+    if (DType<T>::code == ACCRQA_F64) {
+        // float64: the split for the float filter, when the series allows it
+        c.host_hi.resize((size_t)n);
+        c.host_lo.resize((size_t)n);
+        double m = 0.0;
+        if (f64_split((const double *)x, n, c.host_hi.data(), c.host_lo.data(), &m)) {
+            const size_t fb = (size_t)(n + ACCRQA_SERIES_PAD) * sizeof(float);
+            CU(c.series_hi.reserve(fb), "cudaMalloc(series split)");
+            CU(c.series_lo.reserve(fb), "cudaMalloc(series split)");
+            CU(copy_async(c.series_hi.ptr, c.host_hi.data(), (size_t)n * 4, cudaMemcpyHostToDevice,
+                          c.stream), "cudaMemcpy(series split H2D)");
+            CU(copy_async(c.series_lo.ptr, c.host_lo.data(), (size_t)n * 4, cudaMemcpyHostToDevice,
+                          c.stream), "cudaMemcpy(series split H2D)");
+            CU(cudaMemsetAsync((float *)c.series_hi.ptr + n, 0, ACCRQA_SERIES_PAD * 4, c.stream),
+               "cudaMemset(split pad)");
+            CU(cudaMemsetAsync((float *)c.series_lo.ptr + n, 0, ACCRQA_SERIES_PAD * 4, c.stream),
+               "cudaMemset(split pad)");
+            out->hi = (const float *)c.series_hi.ptr;
+            out->lo = (const float *)c.series_lo.ptr;
+            out->maxabs = m;
+        }
+    }
     return SUCCESS;
 }
 
@@ -514,8 +628,9 @@ Accrqa_Error run_rr_in(Context *c, T *out, const T *x, size_t n, const int *taus
     for (int a = 0; a < ntau; a++)
         for (int b = 0; b < nemb; b++)
             if ((err = check_combo(n, taus[a], embs[b]))) return err;
-    const T *d_x = nullptr;
-    if ((err = upload_series<T>(*c, x, (int64_t)n, &d_x))) return err;
+    DevSeries<T> ds;
+    if ((err = upload_series<T>(*c, x, (int64_t)n, &ds))) return err;
+    const T *d_x = ds.x;
     const size_t ncnt = (size_t)ntau * nemb * nthr;
     CU(c->counts.reserve(ncnt * 8), "cudaMalloc(counts)");
     uint64_t *d_counts = (uint64_t *)c->counts.ptr;
@@ -524,7 +639,7 @@ Accrqa_Error run_rr_in(Context *c, T *out, const T *x, size_t n, const int *taus
         for (int b = 0; b < nemb; b++) {
             uint64_t *dst = d_counts + ((size_t)a * nemb + b) * nthr;
             if ((err = enqueue_rr<T>(d_x, (int64_t)n, taus[a], embs[b], thr, nthr, norm,
-                                     dst, c->stream)))
+                                     dst, c->stream, ds.hi, ds.lo, ds.maxabs)))
                 return err;
         }
     trace("RR: %d passes enqueued", ntau * nemb);
@@ -566,8 +681,9 @@ Accrqa_Error run_lines_in(Context *c, int kind, T *out, const T *x, size_t n, co
     const bool full = calc_entr == 1 || lmin_max >= 16;
     const bool is_det = kind == ACCRQA_WALK_DET;
 
-    const T *d_x = nullptr;
-    if ((err = upload_series<T>(*c, x, (int64_t)n, &d_x))) return err;
+    DevSeries<T> ds;
+    if ((err = upload_series<T>(*c, x, (int64_t)n, &ds))) return err;
+    const T *d_x = ds.x;
 
     const size_t budget = line_budget_bytes();
     int combo = 0;
@@ -598,7 +714,8 @@ Accrqa_Error run_lines_in(Context *c, int kind, T *out, const T *x, size_t n, co
             const int64_t nc = embedded_length(n, tau, emb);
             if ((err = enqueue_lines<T>(kind, d_x, (int64_t)n, tau, emb, thr, nthr, norm,
                                         d_hist + off[(size_t)(q - first)], nc + 1,
-                                        d_max + (size_t)(q - first) * nthr, c->stream)))
+                                        d_max + (size_t)(q - first) * nthr, c->stream, ds.hi,
+                                        ds.lo, ds.maxabs)))
                 return err;
         }
         trace("lines: batch [%d, %d) enqueued", first, last);
@@ -703,8 +820,9 @@ Accrqa_Error run_rp(OUT *out, const T *x, size_t n, int tau, int emb, T thr, int
     Context *c = current_context(&err);
     if (!c) return err;
     std::lock_guard<std::mutex> g(c->mu);
-    const T *d_x = nullptr;
-    if ((err = upload_series<T>(*c, x, (int64_t)n, &d_x))) return err;
+    DevSeries<T> ds;
+    if ((err = upload_series<T>(*c, x, (int64_t)n, &ds))) return err;
+    const T *d_x = ds.x;
     const int64_t nc = embedded_length(n, tau, emb);
     const uint64_t key = threshold_key<T>(thr, norm);
     const size_t row_bytes = (size_t)nc * sizeof(OUT);
@@ -740,12 +858,13 @@ Accrqa_Error raw_rr_counts(uint64_t *counts, const T *x, int64_t n, int tau, int
     Context *c = current_context(&err);
     if (!c) return err;
     std::lock_guard<std::mutex> g(c->mu);
-    const T *d_x = nullptr;
-    if ((err = upload_series<T>(*c, x, n, &d_x))) return err;
+    DevSeries<T> ds;
+    if ((err = upload_series<T>(*c, x, n, &ds))) return err;
+    const T *d_x = ds.x;
     CU(c->counts.reserve((size_t)nthr * 8), "cudaMalloc(counts)");
     CU(cudaMemsetAsync(c->counts.ptr, 0, (size_t)nthr * 8, c->stream), "cudaMemset(counts)");
     if ((err = enqueue_rr<T>(d_x, n, tau, emb, thr, nthr, norm, (uint64_t *)c->counts.ptr,
-                             c->stream)))
+                             c->stream, ds.hi, ds.lo, ds.maxabs)))
         return err;
     CU(copy_async(counts, c->counts.ptr, (size_t)nthr * 8, cudaMemcpyDeviceToHost,
                        c->stream), "cudaMemcpy(counts D2H)");
@@ -767,8 +886,9 @@ Accrqa_Error raw_histograms(int kind, uint64_t *hist, const T *x, int64_t n, int
     Context *c = current_context(&err);
     if (!c) return err;
     std::lock_guard<std::mutex> g(c->mu);
-    const T *d_x = nullptr;
-    if ((err = upload_series<T>(*c, x, n, &d_x))) return err;
+    DevSeries<T> ds;
+    if ((err = upload_series<T>(*c, x, n, &ds))) return err;
+    const T *d_x = ds.x;
     const int64_t nc = embedded_length((size_t)n, tau, emb);
     const size_t bytes = (size_t)nthr * (size_t)(nc + 1) * 8;
     CU(c->hist.reserve(bytes), "cudaMalloc(histograms)");
@@ -777,7 +897,7 @@ Accrqa_Error raw_histograms(int kind, uint64_t *hist, const T *x, int64_t n, int
     CU(cudaMemsetAsync(c->maxlen.ptr, 0, (size_t)nthr * 4, c->stream), "cudaMemset(maxlen)");
     if ((err = enqueue_lines<T>(kind, d_x, n, tau, emb, thr, nthr, norm,
                                 (uint64_t *)c->hist.ptr, nc + 1, (uint32_t *)c->maxlen.ptr,
-                                c->stream)))
+                                c->stream, ds.hi, ds.lo, ds.maxabs)))
         return err;
     CU(copy_async(hist, c->hist.ptr, bytes, cudaMemcpyDeviceToHost, c->stream),
        "cudaMemcpy(histograms D2H)");

@@ -44,6 +44,8 @@ struct Context {
     cudaStream_t stream = nullptr;
     std::mutex mu;
     DeviceBuffer series, counts, hist, maxlen, rp[2];
+    DeviceBuffer series_hi, series_lo;         // float split of a float64 series
+    std::vector<float> host_hi, host_lo;
     std::vector<uint64_t> host_u64;
     // batched path: side streams for concurrent launch groups, a device arena
     // for descriptors and results, and pinned staging for one-copy uploads
@@ -73,16 +75,36 @@ template <typename T> struct DType;
 template <> struct DType<float> { static const int32_t code = ACCRQA_F32; };
 template <> struct DType<double> { static const int32_t code = ACCRQA_F64; };
 
+// ---- float64 through the float filter ---------------------------------------
+// Split a float64 series into floats hi = RN(x) and lo = RN(x - hi) and
+// return max|x|.  False (nothing written past the first failing sample) when
+// the series cannot take the filter: a non-finite sample or |x| > 2^60.
+bool f64_split(const double *x, int64_t n, float *hi, float *lo, double *maxabs);
+// The same test and max|x| without writing the split.
+bool f64_filterable(const double *x, int64_t n, double *maxabs);
+// The filter's float limit pair (klo in the low half, khi in the high half)
+// for an exact float64 limit (bits + 1 of the largest passing distance value,
+// 0 when nothing passes), from the error bound of the float evaluation for
+// this norm, emb and max|x|: a float distance v_f < klo is surely
+// recurrent, v_f >= khi surely not, anything between is decided in double.
+uint64_t f64_filter_pair(uint64_t exact_limit, int norm, int emb, double maxabs);
+
 // ---- passes ----------------------------------------------------------------
 // Enqueue the passes for one (series, tau, emb) and nthr thresholds on st.
-// d_counts / d_hist / d_maxlen must be zeroed by the caller.
+// d_counts / d_hist / d_maxlen must be zeroed by the caller.  For float64,
+// d_hi / d_lo (the f64_split of the series, padded like it) and its max|x|
+// select the float-filtered kernels.
 template <typename T>
 Accrqa_Error enqueue_rr(const T *d_x, int64_t n, int tau, int emb, const T *thr,
-                        int nthr, int norm, uint64_t *d_counts, cudaStream_t st);
+                        int nthr, int norm, uint64_t *d_counts, cudaStream_t st,
+                        const float *d_hi = nullptr, const float *d_lo = nullptr,
+                        double maxabs = 0.0);
 template <typename T>
 Accrqa_Error enqueue_lines(int kind, const T *d_x, int64_t n, int tau, int emb,
                            const T *thr, int nthr, int norm, uint64_t *d_hist,
-                           int64_t stride, uint32_t *d_maxlen, cudaStream_t st);
+                           int64_t stride, uint32_t *d_maxlen, cudaStream_t st,
+                           const float *d_hi = nullptr, const float *d_lo = nullptr,
+                           double maxabs = 0.0);
 
 // ---- post-processing --------------------------------------------------------
 // A length histogram H[0..nc] held as a dense prefix H[0..P) plus the single

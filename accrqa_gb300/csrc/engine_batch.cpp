@@ -76,7 +76,7 @@ struct Pass {
 typedef std::tuple<int, int, int, int, int> GroupKey;
 
 int emb_key(int dtype, int emb) {
-    return (dtype == ACCRQA_F32 && emb >= 2 && emb <= 8) ? emb : 0;
+    return ((dtype == ACCRQA_F32 || dtype == ACCRQA_F64F) && emb >= 2 && emb <= 8) ? emb : 0;
 }
 
 template <typename T>
@@ -118,12 +118,22 @@ void write_line_out(void *out, int k, const LineHistogram &h, int lmin, bool ful
 static Accrqa_Error run_batch_part(Context &c, const accrqa_gb300_series_job *jobs, int j0,
                                    int j1) {
     // ---- plan -------------------------------------------------------------
-    std::vector<size_t> xoff((size_t)(j1 - j0));
+    std::vector<size_t> xoff((size_t)(j1 - j0)), hioff((size_t)(j1 - j0), 0);
+    std::vector<double> maxabs((size_t)(j1 - j0), -1.0);   // >= 0: float64 job takes the filter
     size_t series_bytes = 0;
     for (int j = j0; j < j1; j++) {
         const size_t es = jobs[j].dtype == ACCRQA_GB300_F32 ? 4 : 8;
-        xoff[(size_t)(j - j0)] = series_bytes;
+        const size_t jj = (size_t)(j - j0);
+        xoff[jj] = series_bytes;
         series_bytes = align16(series_bytes + (size_t)(jobs[j].n + ACCRQA_SERIES_PAD) * es);
+        double m = 0.0;
+        if (jobs[j].dtype == ACCRQA_GB300_F64 &&
+            f64_filterable((const double *)jobs[j].x, jobs[j].n, &m)) {
+            // float64 job: its float split (hi then lo) follows the series
+            maxabs[jj] = m;
+            hioff[jj] = series_bytes;
+            series_bytes = align16(series_bytes + 2 * (size_t)(jobs[j].n + ACCRQA_SERIES_PAD) * 4);
+        }
     }
     std::vector<Pass> passes;
     for (int j = j0; j < j1; j++) {
@@ -173,7 +183,8 @@ static Accrqa_Error run_batch_part(Context &c, const accrqa_gb300_series_job *jo
         const Pass &p = passes[(size_t)i];
         const accrqa_gb300_series_job &J = jobs[p.job];
         const int nt = p.cnt <= 8 ? 8 : 16;
-        groups[GroupKey(p.kind, J.dtype, J.norm, emb_key(J.dtype, J.emb), nt)].push_back(i);
+        const int dt = maxabs[(size_t)(p.job - j0)] >= 0.0 ? ACCRQA_F64F : J.dtype;
+        groups[GroupKey(p.kind, dt, J.norm, emb_key(dt, J.emb), nt)].push_back(i);
     }
     struct GroupPlan {
         accrqa_batch_launch L;
@@ -224,6 +235,12 @@ static Accrqa_Error run_batch_part(Context &c, const accrqa_gb300_series_job *jo
             for (int k = 0; k < ACCRQA_MAX_THR_PER_PASS; k++) {
                 d.keys[k] = k < p.cnt ? raw[order[k]] : never;
                 if (J.dtype == ACCRQA_GB300_F32) d.keys[k] = accrqa_f32_limit_pair(d.keys[k]);
+                const double m = maxabs[(size_t)(p.job - j0)];
+                if (m >= 0.0) {   // float filter: limit pairs drive the masks
+                    d.xkeys[k] = d.keys[k];
+                    d.keys[k] = k < p.cnt ? f64_filter_pair(d.keys[k], J.norm, J.emb, m)
+                                          : 0xFF800000FF800000ull;
+                }
                 d.row[k] = k < p.cnt ? order[k] : 0;
             }
             d.hist_stride = p.nc + 1;
@@ -277,12 +294,26 @@ static Accrqa_Error run_batch_part(Context &c, const accrqa_gb300_series_job *jo
         char *dst = host + xoff[(size_t)(j - j0)];
         std::memcpy(dst, jobs[j].x, (size_t)jobs[j].n * es);
         std::memset(dst + (size_t)jobs[j].n * es, 0, ACCRQA_SERIES_PAD * es);
+        const size_t jj = (size_t)(j - j0);
+        if (maxabs[jj] >= 0.0) {
+            const int64_t np = jobs[j].n + ACCRQA_SERIES_PAD;
+            float *hi = (float *)(host + hioff[jj]), *lo = hi + np;
+            double m = 0.0;
+            f64_split((const double *)jobs[j].x, jobs[j].n, hi, lo, &m);
+            std::memset(hi + jobs[j].n, 0, ACCRQA_SERIES_PAD * 4);
+            std::memset(lo + jobs[j].n, 0, ACCRQA_SERIES_PAD * 4);
+        }
     }
     for (GroupPlan &gp : plans) {
         for (accrqa_batch_job &d : gp.table) {
             const Pass &p = passes[(size_t)d.pad_];
             d.pad_ = 0;
             d.x = dev + xoff[(size_t)(p.job - j0)];
+            if (maxabs[(size_t)(p.job - j0)] >= 0.0) {
+                const size_t ho = hioff[(size_t)(p.job - j0)];
+                d.xhi = (const float *)(dev + ho);
+                d.xlo = (const float *)(dev + ho) + (jobs[p.job].n + ACCRQA_SERIES_PAD);
+            }
             d.counts = p.kind == ACCRQA_WALK_RR ? (uint64_t *)(dev + p.counts_off) : nullptr;
             d.maxlen = p.kind != ACCRQA_WALK_RR ? (uint32_t *)(dev + p.maxlen_off) : nullptr;
             d.hist = p.kind != ACCRQA_WALK_RR ? (uint64_t *)(dev + p.hist_off) : nullptr;
@@ -408,6 +439,7 @@ size_t batch_job_bytes(const accrqa_gb300_series_job &J) {
     const int64_t nc = J.n - (int64_t)(J.emb - 1) * J.tau;
     const size_t es = J.dtype == ACCRQA_GB300_F32 ? 4 : 8;
     size_t b = (size_t)(J.n + ACCRQA_SERIES_PAD) * es + 4096;
+    if (J.dtype == ACCRQA_GB300_F64) b += 2 * (size_t)(J.n + ACCRQA_SERIES_PAD) * 4;   // float split
     const int lines = (J.det_out ? 1 : 0) + (J.lam_out ? 1 : 0);
     b += (size_t)lines * (size_t)J.nthr * (size_t)(nc + 1) * 8;
     b += (size_t)(nc / 32 + 2) * 16;   // units

@@ -20,6 +20,9 @@ cudaError_t launch_det_f32(const accrqa_walk_desc &, cudaStream_t);
 cudaError_t launch_det_f64(const accrqa_walk_desc &, cudaStream_t);
 cudaError_t launch_lam_f32(const accrqa_walk_desc &, cudaStream_t);
 cudaError_t launch_lam_f64(const accrqa_walk_desc &, cudaStream_t);
+cudaError_t launch_rr_f64f(const accrqa_walk_desc &, cudaStream_t);
+cudaError_t launch_det_f64f(const accrqa_walk_desc &, cudaStream_t);
+cudaError_t launch_lam_f64f(const accrqa_walk_desc &, cudaStream_t);
 
 int sm_count_cached() {
     // One value per device ordinal; the engine only ever uses the current one.
@@ -72,10 +75,17 @@ extern "C" int accrqa_gb300_launch_walk(const accrqa_walk_desc *d, void *stream)
     cudaStream_t st = (cudaStream_t)stream;
     cudaError_t e = cudaErrorInvalidValue;
     const bool f64 = d->dtype == ACCRQA_F64;
+    const bool filt = f64 && d->d_xhi && d->d_xlo;   // float64 through the float filter
     switch (d->kind) {
-        case ACCRQA_WALK_RR: e = f64 ? launch_rr_f64(*d, st) : launch_rr_f32(*d, st); break;
-        case ACCRQA_WALK_DET: e = f64 ? launch_det_f64(*d, st) : launch_det_f32(*d, st); break;
-        case ACCRQA_WALK_LAM: e = f64 ? launch_lam_f64(*d, st) : launch_lam_f32(*d, st); break;
+        case ACCRQA_WALK_RR:
+            e = filt ? launch_rr_f64f(*d, st) : f64 ? launch_rr_f64(*d, st) : launch_rr_f32(*d, st);
+            break;
+        case ACCRQA_WALK_DET:
+            e = filt ? launch_det_f64f(*d, st) : f64 ? launch_det_f64(*d, st) : launch_det_f32(*d, st);
+            break;
+        case ACCRQA_WALK_LAM:
+            e = filt ? launch_lam_f64f(*d, st) : f64 ? launch_lam_f64(*d, st) : launch_lam_f32(*d, st);
+            break;
         default: break;
     }
     return (int)e;

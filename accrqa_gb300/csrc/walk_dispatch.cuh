@@ -16,6 +16,9 @@ namespace accrqa {
 int sm_count_cached();
 extern std::atomic<unsigned long long> g_launches;
 
+// Filter limit pair of a padding slot: (-inf, -inf), surely not recurrent.
+constexpr u64 kNeverFilterPair = 0xFF800000FF800000ull;
+
 template <int KIND, typename T, int NORM, int EMB, int NT>
 static cudaError_t launch_one(const accrqa_walk_desc &d, cudaStream_t st) {
     void (*kern)(WalkArgs);
@@ -67,10 +70,20 @@ static cudaError_t launch_one(const accrqa_walk_desc &d, cudaStream_t st) {
             order[q - 1] = t;
         }
     for (int k = 0; k < kMaxThrPerPass; k++) {
-        a.keys[k] = d.dtype == ACCRQA_F32 ? accrqa_f32_limit_pair(d.keys[order[k]])
-                                          : d.keys[order[k]];
+        if (std::is_same<T, F64F>::value) {
+            // float filter: its limit pairs drive the masks, the exact
+            // float64 limits decide the ambiguous cells
+            a.keys[k] = order[k] < d.nthr ? d.filter_keys[order[k]] : kNeverFilterPair;
+            a.xkeys[k] = d.keys[order[k]];
+        } else {
+            a.keys[k] = d.dtype == ACCRQA_F32 ? accrqa_f32_limit_pair(d.keys[order[k]])
+                                              : d.keys[order[k]];
+            a.xkeys[k] = 0;
+        }
         a.row[k] = order[k] < d.nthr ? order[k] : 0;
     }
+    a.xhi = (const float *)d.d_xhi;
+    a.xlo = (const float *)d.d_xlo;
     a.counts = (u64 *)d.d_counts;
     a.hist = (u64 *)d.d_hist;
     a.hist_stride = d.hist_stride;

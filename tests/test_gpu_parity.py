@@ -107,3 +107,29 @@ def test_rp_matches_oracle(gpu, oracle_mod, dt):
     x64 = x.astype(np.float64)
     np.testing.assert_array_equal(gpu.rp(x64, 2, 3, 0.5, 1, out_dtype=np.int32),
                                   oracle_mod.rp_i32(x64, 2, 3, 0.5, 1))
+
+
+@pytest.mark.parametrize("scale,offset,grid", [(1.0, 0.0, False), (1.0, 0.0, True),
+                                               (1e6, 0.0, True), (1e-12, 0.0, False),
+                                               (1.0, 1e9, False), (1e100, 0.0, False)])
+def test_f64_filter_matches_oracle(gpu, oracle_mod, scale, offset, grid):
+    """float64 passes decide cells in float against proven limits and only
+    the cells near a threshold in double.  Scales and offsets move the
+    bound's relative and absolute parts (offset 1e9 makes most cells
+    ambiguous), the grid puts many distances exactly on thresholds, and
+    |x| = 1e100 turns the filter off."""
+    x0 = workloads.lorenz_x(600, 9, transient=500)
+    x0 = x0 / np.std(x0)
+    if grid:
+        x0 = np.round(x0 * 16) / 16
+    x = x0 * scale + offset
+    thr = np.array([0.0, 0.0625, 0.125, 0.3, 0.5, 0.75, 1.5]) * scale
+    for norm in NORMS:
+        for tau, emb in [(1, 3), (2, 5), (1, 1)]:
+            np.testing.assert_array_equal(gpu.rr_counts(x, tau, emb, thr, norm),
+                                          oracle_mod.rr_counts(x, tau, emb, thr, norm))
+            det = gpu.det_histograms(x, tau, emb, thr, norm)
+            lam = gpu.lam_histograms(x, tau, emb, thr, norm)
+            for k, t in enumerate(thr):
+                np.testing.assert_array_equal(det[k], oracle_mod.det_hist(x, tau, emb, t, norm))
+                np.testing.assert_array_equal(lam[k], oracle_mod.lam_hist(x, tau, emb, t, norm))

@@ -74,6 +74,10 @@ def _declare(lib: ctypes.CDLL) -> None:
         f = getattr(lib, name)
         f.argtypes = [vp, i64, vp, vp, i32, i64, i32, i32, vp, i32, i32, vp]
         f.restype = ctypes.c_int
+    lib.accrqa_gb300_rp_bits.argtypes = [vp, vp, i32, i64, i32, i32, ctypes.c_double, i32]
+    lib.accrqa_gb300_rp_bits.restype = ctypes.c_int
+    lib.accrqa_gb300_rp_bits_dev.argtypes = [vp, vp, i32, i64, i32, i32, ctypes.c_double, i32, vp]
+    lib.accrqa_gb300_rp_bits_dev.restype = ctypes.c_int
     lib.accrqa_gb300_probe_fp32.argtypes = [i32, i32, ctypes.POINTER(ctypes.c_double)]
     lib.accrqa_gb300_probe_fp32.restype = ctypes.c_int
 

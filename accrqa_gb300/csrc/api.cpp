@@ -295,6 +295,18 @@ Accrqa_Error accrqa_gb300_rp(void *out, int32_t out_type, const void *x, int32_t
     return ERR_DATA_TYPE;
 }
 
+Accrqa_Error accrqa_gb300_rp_bits(uint32_t *out, const void *x, int32_t dtype, int64_t n,
+                                  int32_t tau, int32_t emb, double threshold, int32_t norm) {
+    if (!out || !x) return ERR_MEM_ALLOC_FAILURE;
+    if (n <= 0) return ERR_INVALID_ARGUMENT;
+    if (dtype == ACCRQA_GB300_F32)
+        return run_rp_bits<float>(out, (const float *)x, (size_t)n, tau, emb, (float)threshold,
+                                  norm);
+    if (dtype == ACCRQA_GB300_F64)
+        return run_rp_bits<double>(out, (const double *)x, (size_t)n, tau, emb, threshold, norm);
+    return ERR_DATA_TYPE;
+}
+
 Accrqa_Error accrqa_gb300_measures(double *out5, const uint64_t *hist, int64_t hs,
                                    int64_t lmin, int32_t is_det) {
     if (!out5 || !hist) return ERR_MEM_ALLOC_FAILURE;
@@ -362,6 +374,20 @@ Accrqa_Error accrqa_gb300_lam_hist_dev(uint64_t *d_hist, int64_t stride, uint32_
                                        int32_t nthr, int32_t norm, void *stream) {
     return lines_dev(ACCRQA_WALK_LAM, d_hist, stride, d_maxlen, d_x, dtype, n, tau, emb,
                      thresholds, nthr, norm, stream);
+}
+
+Accrqa_Error accrqa_gb300_rp_bits_dev(uint32_t *d_out, const void *d_x, int32_t dtype,
+                                      int64_t n, int32_t tau, int32_t emb, double threshold,
+                                      int32_t norm, void *stream) {
+    if (!d_out || !d_x) return ERR_MEM_ALLOC_FAILURE;
+    Accrqa_Error e = dev_common(dtype, n, tau, emb, 1, norm);
+    if (e) return e;
+    const int64_t nc = n - (int64_t)(emb - 1) * tau;
+    const uint64_t key = dtype == ACCRQA_GB300_F32 ? threshold_key_f32((float)threshold, norm)
+                                                   : threshold_key_f64(threshold, norm);
+    const int le = accrqa_gb300_launch_rp_bits(d_x, dtype == ACCRQA_GB300_F32 ? ACCRQA_F32 : ACCRQA_F64,
+                                               norm, nc, tau, emb, key, d_out, 0, nc, stream);
+    return le ? cuda_error((cudaError_t)le, "bit-packed RP kernel launch") : SUCCESS;
 }
 
 }  // extern "C"

@@ -845,6 +845,37 @@ Accrqa_Error run_rp(OUT *out, const T *x, size_t n, int tau, int emb, T thr, int
 }
 
 template <typename T>
+Accrqa_Error run_rp_bits(uint32_t *out, const T *x, size_t n, int tau, int emb, T thr,
+                         int norm) {
+    Accrqa_Error err = check_norm(norm);
+    if (err) return err;
+    if ((err = check_combo(n, tau, emb))) return err;
+    err = SUCCESS;
+    Context *c = current_context(&err);
+    if (!c) return err;
+    std::lock_guard<std::mutex> g(c->mu);
+    DevSeries<T> ds;
+    if ((err = upload_series<T>(*c, x, (int64_t)n, &ds))) return err;
+    const int64_t nc = embedded_length(n, tau, emb);
+    const uint64_t key = threshold_key<T>(thr, norm);
+    const size_t row_bytes = (size_t)((nc + 31) / 32) * 4;
+    int64_t rows = (int64_t)(((size_t)256 << 20) / row_bytes);
+    if (rows < 1) rows = 1;
+    if (rows > nc) rows = nc;
+    CU(c->rp[0].reserve((size_t)rows * row_bytes), "cudaMalloc(RP chunk)");
+    for (int64_t r0 = 0; r0 < nc; r0 += rows) {
+        const int64_t nr = nc - r0 < rows ? nc - r0 : rows;
+        int e = accrqa_gb300_launch_rp_bits(ds.x, DType<T>::code, norm, nc, tau, emb, key,
+                                            c->rp[0].ptr, r0, nr, c->stream);
+        if (e) return cuda_error((cudaError_t)e, "bit-packed RP kernel launch");
+        CU(copy_async((char *)out + (size_t)r0 * row_bytes, c->rp[0].ptr, (size_t)nr * row_bytes,
+                      cudaMemcpyDeviceToHost, c->stream), "cudaMemcpy(RP D2H)");
+        CU(cudaStreamSynchronize(c->stream), "bit-packed RP kernel");
+    }
+    return SUCCESS;
+}
+
+template <typename T>
 Accrqa_Error raw_rr_counts(uint64_t *counts, const T *x, int64_t n, int tau, int emb,
                            const T *thr, int nthr, int norm) {
     Accrqa_Error err = check_norm(norm);
@@ -917,6 +948,8 @@ template Accrqa_Error run_rr<float>(float *, const float *, size_t, const int *,
 template Accrqa_Error run_rr<double>(double *, const double *, size_t, const int *, int, const int *, int, const double *, int, int);
 template Accrqa_Error run_lines<float>(int, float *, const float *, size_t, const int *, int, const int *, int, const int *, int, const float *, int, int, int);
 template Accrqa_Error run_lines<double>(int, double *, const double *, size_t, const int *, int, const int *, int, const int *, int, const double *, int, int, int);
+template Accrqa_Error run_rp_bits<float>(uint32_t *, const float *, size_t, int, int, float, int);
+template Accrqa_Error run_rp_bits<double>(uint32_t *, const double *, size_t, int, int, double, int);
 template Accrqa_Error run_rp<float, char>(char *, const float *, size_t, int, int, float, int);
 template Accrqa_Error run_rp<float, int>(int *, const float *, size_t, int, int, float, int);
 template Accrqa_Error run_rp<double, char>(char *, const double *, size_t, int, int, double, int);

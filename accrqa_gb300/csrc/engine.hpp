@@ -143,6 +143,10 @@ Accrqa_Error run_lines(int kind, T *out, const T *x, size_t n, const int *taus,
 template <typename T, typename OUT>
 Accrqa_Error run_rp(OUT *out, const T *x, size_t n, int tau, int emb, T thr,
                     int norm);
+// Bit-packed RP: nc rows of ceil(nc/32) words (bit c of word w = column 32w+c).
+template <typename T>
+Accrqa_Error run_rp_bits(uint32_t *out, const T *x, size_t n, int tau, int emb, T thr,
+                         int norm);
 
 // One series job through the per-series path, on a given context.
 Accrqa_Error run_job_plain(Context &c, const accrqa_gb300_series_job &job);

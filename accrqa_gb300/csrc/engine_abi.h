@@ -75,6 +75,12 @@ int accrqa_gb300_launch_rp(const void *d_x, int32_t dtype, int32_t norm,
                            void *d_out, int32_t out_type, int64_t row0,
                            int64_t nrows, void *stream);
 
+/* The same, bit-packed: rows of ceil(nc/32) uint32 words, bit c of word w of
+ * a row = column 32*w + c (bits past nc are 0). */
+int accrqa_gb300_launch_rp_bits(const void *d_x, int32_t dtype, int32_t norm,
+                                int64_t nc, int32_t tau, int32_t emb, uint64_t key,
+                                void *d_out, int64_t row0, int64_t nrows, void *stream);
+
 /* Number of streaming multiprocessors of the current device (cached). */
 int accrqa_gb300_sm_count(void);
 

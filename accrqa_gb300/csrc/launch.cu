@@ -61,7 +61,41 @@ static cudaError_t launch_rp_t(const void *d_x, int norm, long long nc, int tau,
     return cudaGetLastError();
 }
 
+template <typename T>
+static cudaError_t launch_rp_bits_t(const void *d_x, int norm, long long nc, int tau, int emb,
+                                    u64 key, void *d_out, long long row0, long long nrows,
+                                    cudaStream_t st) {
+    const long long words = nrows * ((nc + 31) / 32);
+    const int threads = 256;
+    const long long blocks = (words + threads - 1) / threads;
+    if (blocks <= 0) return cudaSuccess;
+    if (blocks > 0x7FFFFFFFll) return cudaErrorInvalidValue;
+    if (norm == kNormEuclidean)
+        rp_bits<T, kNormEuclidean><<<(unsigned)blocks, threads, 0, st>>>(
+            (const T *)d_x, nc, tau, emb, key, (u32 *)d_out, row0, nrows);
+    else if (norm == kNormMaximal)
+        rp_bits<T, kNormMaximal><<<(unsigned)blocks, threads, 0, st>>>(
+            (const T *)d_x, nc, tau, emb, key, (u32 *)d_out, row0, nrows);
+    else
+        return cudaErrorInvalidValue;
+    g_launches.fetch_add(1);
+    return cudaGetLastError();
+}
+
 }  // namespace accrqa
+
+extern "C" int accrqa_gb300_launch_rp_bits(const void *d_x, int32_t dtype, int32_t norm,
+                                           int64_t nc, int32_t tau, int32_t emb, uint64_t key,
+                                           void *d_out, int64_t row0, int64_t nrows,
+                                           void *stream) {
+    using namespace accrqa;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (dtype == ACCRQA_F32)
+        return (int)launch_rp_bits_t<float>(d_x, norm, nc, tau, emb, key, d_out, row0, nrows, st);
+    if (dtype == ACCRQA_F64)
+        return (int)launch_rp_bits_t<double>(d_x, norm, nc, tau, emb, key, d_out, row0, nrows, st);
+    return (int)cudaErrorInvalidValue;
+}
 
 extern "C" int accrqa_gb300_sm_count(void) { return accrqa::sm_count_cached(); }
 

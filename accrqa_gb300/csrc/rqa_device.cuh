@@ -239,8 +239,11 @@ template <> __device__ __forceinline__ double never_value<double>() { return __l
 constexpr int kGroup = 8;
 
 // float: four cell pairs.  d = v - lim on the f32x2 pipe, then one funnel
-// shift per cell moves its sign bit (recurrent) into the mask.
-template <int NT>
+// shift per cell moves its sign bit (recurrent) into the mask.  With STOP
+// (the LAM walker, where it measured faster) the warp checks every fourth
+// slot whether any lane still has a recurrent cell in the group and stops
+// pushing when none has.
+template <int NT, bool STOP = false>
 __device__ __forceinline__ void push_group(u32 (&m)[NT], const f2 (&v)[kGroup / 2],
                                            const u64 (&keys)[kMaxThrPerPass]) {
     f2 d0[kGroup / 2];
@@ -263,17 +266,31 @@ __device__ __forceinline__ void push_group(u32 (&m)[NT], const f2 (&v)[kGroup / 
     }
 #pragma unroll
     for (int k = 1; k < NT; k++) {
+        f2 d[kGroup / 2];
+        u64 anyk = 0;
 #pragma unroll
         for (int q = 0; q < kGroup / 2; q++) {
-            const f2 d = sub2(v[q], keys[k]);
-            m[k] = __funnelshift_l((u32)d, m[k], 1);
-            m[k] = __funnelshift_l((u32)(d >> 32), m[k], 1);
+            d[q] = sub2(v[q], keys[k]);
+            anyk |= d[q];
+        }
+        // every fourth slot: once no lane has a recurrent cell of the group
+        // here, the narrower slots have none either (nested) -- shift zeros
+        if (STOP && (k & 3) == 0 &&
+            !__any_sync(0xFFFFFFFFu, ((u32)anyk | (u32)(anyk >> 32)) >> 31)) {
+#pragma unroll
+            for (int kk = k; kk < NT; kk++) m[kk] <<= kGroup;
+            return;
+        }
+#pragma unroll
+        for (int q = 0; q < kGroup / 2; q++) {
+            m[k] = __funnelshift_l((u32)d[q], m[k], 1);
+            m[k] = __funnelshift_l((u32)(d[q] >> 32), m[k], 1);
         }
     }
 }
 
 // double: an integer compare of the bit pattern against the limit.
-template <int NT>
+template <int NT, bool STOP = false>
 __device__ __forceinline__ void push_group(u32 (&m)[NT], const double (&v)[kGroup],
                                            const u64 (&keys)[kMaxThrPerPass]) {
     u64 lo = (u64)__double_as_longlong(v[0]);

@@ -32,8 +32,9 @@
 namespace accrqa {
 
 constexpr int kWarpsPerCta = 4;
-// Resident CTAs per SM the line kernels are compiled for (register cap): the
-// diagonal walker waits on loads and needs the warps to hide them.
+// Resident CTAs per SM the diagonal walker is compiled for (register cap, 80
+// registers): it waits on two loads per cell and dimension and needs the
+// warps to hide them.
 constexpr int kLineMinCtas = 6;
 constexpr int kSeriesPad = 128;
 
@@ -329,7 +330,7 @@ __device__ __forceinline__ void exact_fixup(u32 (&m)[NT], u32 amb, const double 
 }
 
 // The masks of one 32-cell block of a row (cells xj[0..32)).
-template <typename T, int NORM, int EMB, int NT, bool CHECK>
+template <typename T, int NORM, int EMB, int NT, bool CHECK, bool STOP = false>
 __device__ __forceinline__ void row_masks(u32 (&m)[NT], const LaneVec<T, EMB> &a,
                                           typename SeriesOf<T>::ptr xi,
                                           typename SeriesOf<T>::ptr xj,
@@ -347,7 +348,7 @@ __device__ __forceinline__ void row_masks(u32 (&m)[NT], const LaneVec<T, EMB> &a
                 exact_fixup<NORM, EMB, NT>(m, amb, exact_ptr(xi), 0, exact_ptr(xj) + g, tau, emb,
                                            xkeys);
         } else {
-            push_group<NT>(m, v, keys);
+            push_group<NT, STOP>(m, v, keys);
         }
     }
 }
@@ -584,7 +585,7 @@ __device__ __forceinline__ void lam_block(const LaneVec<T, EMB> &a,
                                           const u64 (&keys)[kMaxThrPerPass], const u64 *xkeys,
                                           u32 (&carry)[NT], const Sink &sink) {
     u32 m[NT];
-    row_masks<T, NORM, EMB, NT, CHECK>(m, a, xi, xj, tau, emb, 0, rem, keys, xkeys);
+    row_masks<T, NORM, EMB, NT, CHECK, true>(m, a, xi, xj, tau, emb, 0, rem, keys, xkeys);
     close_block<NT, Sink>(m, carry, sink);
 }
 
@@ -652,6 +653,30 @@ __global__ void rp_cells(const T *__restrict__ x, long long nc, int tau, int emb
             out[r * nc + j] = is_rec(v, key) ? OUT(1) : OUT(0);
         }
     }
+}
+
+// ---------------------------------------------------------------------------
+// RP, bit-packed: one thread per 32-cell word of a row; bit c of word w of
+// row r is cell (row0 + r, 32*w + c), bits past nc are 0.  A row takes
+// ceil(nc/32) words: 1/8 of the byte plot's memory and copy.
+// ---------------------------------------------------------------------------
+template <typename T, int NORM>
+__global__ void rp_bits(const T *__restrict__ x, long long nc, int tau, int emb, u64 key,
+                        u32 *__restrict__ out, long long row0, long long nrows) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long wpr = (nc + 31) / 32;
+    const long long r = idx / wpr;
+    if (r >= nrows) return;
+    const long long w = idx - r * wpr;
+    const long long i = row0 + r;
+    u32 bits = 0;
+#pragma unroll 4
+    for (int c = 0; c < 32; c++) {
+        const long long j = w * 32 + c;
+        if (j < nc && is_rec(cell_dist_mem<T, NORM, 0>(x + i, x + j, tau, emb), key))
+            bits |= 1u << c;
+    }
+    out[r * wpr + w] = bits;
 }
 
 }  // namespace accrqa

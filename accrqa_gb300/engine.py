@@ -114,6 +114,33 @@ def rp(x, tau: int, emb: int, threshold: float, norm, out_dtype=np.int8) -> np.n
     return out
 
 
+def rp_bits(x, tau: int, emb: int, threshold: float, norm) -> np.ndarray:
+    """Bit-packed recurrence plot: uint32 [nc][ceil(nc/32)], bit c of word w
+    of row i = cell (i, 32*w + c)."""
+    x = np.ascontiguousarray(x)
+    nc = embedded_length(len(x), tau, emb)
+    out = np.zeros((max(nc, 0), max((nc + 31) // 32, 0)), dtype=np.uint32)
+    _check(_lib.handle().accrqa_gb300_rp_bits(
+        _vp(out), _vp(x), _dtype_code(x), len(x), tau, emb, float(threshold), _norm(norm)),
+        "rp_bits")
+    return out
+
+
+def rp_bits_dev(d_out: int, d_x: int, dtype_code: int, n: int, tau: int, emb: int,
+                threshold: float, norm, stream: int = 0) -> None:
+    """Enqueue the bit-packed plot of a device series (>= n + 128 elements)
+    into device memory d_out (nc * ceil(nc/32) uint32) on `stream`."""
+    _check(_lib.handle().accrqa_gb300_rp_bits_dev(
+        ctypes.c_void_p(d_out), ctypes.c_void_p(d_x), dtype_code, n, tau, emb, float(threshold),
+        _norm(norm), ctypes.c_void_p(stream)), "rp_bits_dev")
+
+
+def unpack_rp_bits(bits: np.ndarray, nc: int) -> np.ndarray:
+    """int8 [nc][nc] plot from its bit-packed form."""
+    b = np.unpackbits(bits.view(np.uint8).reshape(bits.shape[0], -1), axis=1, bitorder="little")
+    return b[:, :nc].astype(np.int8)
+
+
 def measures(hist, lmin: int, is_det: bool) -> np.ndarray:
     """{DET|LAM, L|TT, Lmax|TTmax, ENTR, RR} of one histogram (float64)."""
     h = np.ascontiguousarray(hist, dtype=np.uint64)

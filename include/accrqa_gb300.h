@@ -237,6 +237,13 @@ Accrqa_Error accrqa_gb300_rp(void *out, int32_t out_type, const void *x,
                              int32_t dtype, int64_t n, int32_t tau,
                              int32_t emb, double threshold, int32_t norm);
 
+/* Recurrence plot, bit-packed (no counterpart in the reference, which has
+ * only the byte/int plot): nc rows of ceil(nc/32) uint32 words, bit c of word
+ * w of row i = cell (i, 32*w + c), bits past nc are 0 -- 1/8 of the int8
+ * plot's memory and transfer.  Same threshold conversion as accrqa_gb300_rp. */
+Accrqa_Error accrqa_gb300_rp_bits(uint32_t *out, const void *x, int32_t dtype, int64_t n,
+                                  int32_t tau, int32_t emb, double threshold, int32_t norm);
+
 /* The five measures {DET|LAM, L|TT, Lmax|TTmax, ENTR, RR} of one histogram
  * hist[0..hs) for minimal line length lmin, as doubles
  * (src/AccRQA_functions.cpp:48-133).  is_det selects the DET search for the
@@ -322,6 +329,13 @@ int64_t accrqa_gb300_server_submit(accrqa_gb300_server *s, const accrqa_gb300_se
 Accrqa_Error accrqa_gb300_server_wait(accrqa_gb300_server *s, int64_t ticket, double *latency_ms);
 void accrqa_gb300_server_stats(accrqa_gb300_server *s, uint64_t *batches, uint64_t *served);
 void accrqa_gb300_server_destroy(accrqa_gb300_server *s);
+
+/* The bit-packed recurrence plot of a device-resident series (>= n + 128
+ * elements) into d_out (nc * ceil(nc/32) words, device memory), enqueued on
+ * `stream`; for serving loops that keep plots in HBM. */
+Accrqa_Error accrqa_gb300_rp_bits_dev(uint32_t *d_out, const void *d_x, int32_t dtype,
+                                      int64_t n, int32_t tau, int32_t emb, double threshold,
+                                      int32_t norm, void *stream);
 
 /* Recurrence rate for callers that cannot allocate device memory.  No
  * counterpart in the reference: it exists for callers that may not call

@@ -204,3 +204,32 @@ def test_rr_target_equals_one_step_per_call(gpu, dt):
                           threshold_min=tmin, threshold_max=tmax)
         want = _rr_target_one_step_per_call(x, 2, 3, target, D, eps, max_iter, tmin, tmax)
         assert got[0] == want[0] and got[1] == want[1], (target, eps, got, want)
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_rp_bits_equal_byte_plot(gpu, dt):
+    """The bit-packed plot (host and device-resident) holds the byte plot's
+    cells, including a row length that is not a multiple of 32."""
+    import torch
+    from accrqa_gb300 import engine
+    x = workloads.lorenz_x(1500, 4, transient=500).astype(dt)
+    for norm in (1, 2):
+        for tau, emb, t in [(1, 3, 0.4), (2, 5, 1.1), (3, 1, 0.0)]:
+            nc = len(x) - (emb - 1) * tau
+            full = engine.rp(x, tau, emb, t, norm)
+            bits = engine.rp_bits(x, tau, emb, t, norm)
+            assert bits.shape == (nc, (nc + 31) // 32)
+            np.testing.assert_array_equal(engine.unpack_rp_bits(bits, nc), full)
+            # padding bits past nc are zero
+            if nc % 32:
+                assert not np.any(bits[:, -1] >> np.uint32(nc % 32))
+            dx = torch.zeros(len(x) + 128, dtype=torch.float32 if dt == np.float32 else torch.float64,
+                             device="cuda")
+            dx[:len(x)].copy_(torch.from_numpy(x))
+            dout = torch.zeros(nc * ((nc + 31) // 32), dtype=torch.int32, device="cuda")
+            s = torch.cuda.current_stream()
+            engine.rp_bits_dev(dout.data_ptr(), dx.data_ptr(), 0 if dt == np.float32 else 1,
+                               len(x), tau, emb, t, norm, s.cuda_stream)
+            torch.cuda.synchronize()
+            np.testing.assert_array_equal(dout.cpu().numpy().view(np.uint32).reshape(bits.shape),
+                                          bits)

@@ -737,7 +737,7 @@ def main(argv=None):
 
     ap.add_argument("--batch-series", type=int, default=512)
     ap.add_argument("--skip-served", action="store_true")
-    ap.add_argument("--serve-rates", type=lambda s: [float(v) for v in s.split(",")], default=[20.0, 60.0])
+    ap.add_argument("--serve-rates", type=lambda s: [float(v) for v in s.split(",")], default=[20.0, 60.0, 120.0])
     ap.add_argument("--serve-requests", type=int, default=120)
     ap.add_argument("--serve-workers", type=int, default=4)
     args = ap.parse_args(argv)

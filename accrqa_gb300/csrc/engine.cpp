@@ -1,6 +1,7 @@
 // engine.cpp -- host side of the GB300 RQA engine (see engine.hpp).
 #include "engine.hpp"
 
+#include <algorithm>
 #include <atomic>
 #include <cfloat>
 #include <chrono>
@@ -379,46 +380,69 @@ template Accrqa_Error enqueue_lines<double>(int, const double *, int64_t, int, i
 // ===========================================================================
 // Histogram post-processing
 // ===========================================================================
-LineHistogram::LineHistogram(std::vector<uint64_t> prefix, uint64_t h_last,
-                             int64_t nc)
-    : h_(std::move(prefix)), h_last_(h_last), nc_(nc) {
-    p_ = (int64_t)h_.size();
-    if (p_ > nc_ + 1) {
-        h_.resize((size_t)(nc_ + 1));
-        p_ = nc_ + 1;
+LineHistogram::LineHistogram(const std::vector<uint64_t> &prefix, uint64_t h_last, int64_t nc)
+    : nc_(nc) {
+    int64_t p = (int64_t)prefix.size();
+    if (p > nc + 1) p = nc + 1;
+    for (int64_t l = 0; l < p; l++) {
+        const uint64_t v = prefix[(size_t)l];
+        if (v) {
+            len_.push_back(l);
+            cnt_.push_back(v);
+        }
     }
-    if (p_ == nc_ + 1) h_last_ = h_[(size_t)nc_];
-    m_.resize((size_t)p_);
-    s_.resize((size_t)p_);
+    if (p <= nc && h_last) {
+        len_.push_back(nc);
+        cnt_.push_back(h_last);
+    }
+    build_sums();
+}
+
+LineHistogram::LineHistogram(std::vector<std::pair<int64_t, uint64_t>> bins, int64_t nc)
+    : nc_(nc) {
+    len_.reserve(bins.size());
+    cnt_.reserve(bins.size());
+    for (const auto &b : bins) {
+        if (b.second && b.first >= 0 && b.first <= nc) {
+            len_.push_back(b.first);
+            cnt_.push_back(b.second);
+        }
+    }
+    build_sums();
+}
+
+void LineHistogram::build_sums() {
+    const size_t k = len_.size();
+    m_.assign(k, 0);
+    s_.assign(k, 0);
     uint64_t m = 0, s = 0;
-    if (p_ <= nc_) {
-        m = (uint64_t)nc_ * h_last_;
-        s = h_last_;
-    }
-    for (int64_t l = p_ - 1; l >= 0; l--) {
-        m += (uint64_t)l * h_[(size_t)l];
-        s += h_[(size_t)l];
-        m_[(size_t)l] = m;
-        s_[(size_t)l] = s;
+    for (size_t i = k; i-- > 0;) {
+        m += (uint64_t)len_[i] * cnt_[i];
+        s += cnt_[i];
+        m_[i] = m;
+        s_[i] = s;
     }
 }
 
+size_t LineHistogram::first_at_least(int64_t l) const {
+    return (size_t)(std::lower_bound(len_.begin(), len_.end(), l) - len_.begin());
+}
+
 uint64_t LineHistogram::bin(int64_t l) const {
-    if (l >= 0 && l < p_) return h_[(size_t)l];
-    if (l == nc_) return h_last_;
-    return 0;
+    const size_t i = first_at_least(l);
+    return (i < len_.size() && len_[i] == l) ? cnt_[i] : 0;
 }
 
 uint64_t LineHistogram::metric(int64_t l) const {
     if (l < 0 || l > nc_) return 0;
-    if (l < p_) return m_[(size_t)l];
-    return (uint64_t)nc_ * h_last_;
+    const size_t i = first_at_least(l);
+    return i < len_.size() ? m_[i] : 0;
 }
 
 uint64_t LineHistogram::scan(int64_t l) const {
     if (l < 0 || l > nc_) return 0;
-    if (l < p_) return s_[(size_t)l];
-    return h_last_;
+    const size_t i = first_at_least(l);
+    return i < len_.size() ? s_[i] : 0;
 }
 
 // src/AccRQA_functions.cpp:48-58
@@ -465,21 +489,13 @@ double LineHistogram::tertiary(int is_det) const {
 }
 
 // Entropy over lengths >= lmin (src/AccRQA_functions.cpp:114-124).  Zero
-// bins add nothing (p > 0 fails, also for 0/0), so only the non-zero prefix
-// and the last bin are visited, in ascending order as in the reference.
+// bins add nothing (p > 0 fails, also for 0/0), so only the non-zero bins are
+// visited, in ascending length as in the reference.
 double LineHistogram::quaternary(int64_t lmin) const {
     double entr = 0;
     const double denom = (double)scan(lmin);
-    int64_t f = lmin < 0 ? 0 : lmin;
-    for (; f < p_; f++) {
-        double p = (double)h_[(size_t)f] / denom;
-        if (p > 0) {
-            double t = p * std::log(p);
-            entr = entr + t;
-        }
-    }
-    if (p_ <= nc_ && lmin <= nc_) {
-        double p = (double)h_last_ / denom;
+    for (size_t i = first_at_least(lmin < 0 ? 0 : lmin); i < len_.size(); i++) {
+        double p = (double)cnt_[i] / denom;
         if (p > 0) {
             double t = p * std::log(p);
             entr = entr + t;
@@ -579,41 +595,70 @@ static size_t line_budget_bytes() {
     return b < cap ? b : cap;
 }
 
-// Copy back the non-zero prefix of nthr histograms and wrap them.
+// Fetch nthr histograms (rows of nc+1 bins at `stride`) and wrap them: the
+// device compacts the non-zero bins and only those come back (a few hundred KB
+// where the dense rows are tens of MB); when more than a quarter of the bins
+// are non-zero the dense rows are copied instead.  DET rows hold the raw
+// upper-triangle runs: they are doubled and get the line of identity
+// (src/AccRQA_CPU_function.cpp:156-162).
 static Accrqa_Error fetch_histograms(Context &c, int kind, const uint64_t *d_hist,
-                                     int64_t stride, const uint32_t *d_maxlen,
-                                     int nthr, int64_t nc,
+                                     int64_t stride, int nthr, int64_t nc,
                                      std::vector<LineHistogram> &out) {
-    std::vector<uint32_t> maxlen((size_t)nthr);
-    CU(copy_async(maxlen.data(), d_maxlen, (size_t)nthr * 4, cudaMemcpyDeviceToHost,
-                       c.stream), "cudaMemcpy(maxlen D2H)");
+    const bool is_det = kind == ACCRQA_WALK_DET;
+    const int64_t p = nc + 1;
+    const int64_t cap = std::max<int64_t>(1024, p * nthr / 4);
+    CU(c.pairs.reserve((size_t)cap * 16), "cudaMalloc(histogram pairs)");
+    CU(c.pair_count.reserve(8), "cudaMalloc(pair count)");
+    CU(cudaMemsetAsync(c.pair_count.ptr, 0, 8, c.stream), "cudaMemset(pair count)");
+    int e = accrqa_gb300_launch_compact(d_hist, stride, nthr, p, (uint64_t *)c.pairs.ptr, cap,
+                                        (unsigned long long *)c.pair_count.ptr, c.stream);
+    if (e) return cuda_error((cudaError_t)e, "histogram compaction");
+    unsigned long long total = 0;
+    CU(copy_async(&total, c.pair_count.ptr, 8, cudaMemcpyDeviceToHost, c.stream),
+       "cudaMemcpy(pair count D2H)");
     CU(cudaStreamSynchronize(c.stream), "line kernels");
-    trace("fetch: kernels done (nc=%lld)", (long long)nc);
-    uint32_t mx = 0;
-    for (uint32_t v : maxlen) mx = v > mx ? v : mx;
-    int64_t p = (int64_t)(mx + 1 > ACCRQA_SHORT_RUN_BINS ? mx + 1 : ACCRQA_SHORT_RUN_BINS);
-    if (p > nc + 1) p = nc + 1;
+    trace("fetch: kernels done (nc=%lld, %llu non-zero bins)", (long long)nc, total);
+    out.clear();
+    out.reserve((size_t)nthr);
+    if ((int64_t)total <= cap) {
+        std::vector<uint64_t> pr((size_t)total * 2);
+        if (total)
+            CU(copy_async(pr.data(), c.pairs.ptr, (size_t)total * 16, cudaMemcpyDeviceToHost,
+                          c.stream), "cudaMemcpy(histogram pairs D2H)");
+        CU(cudaStreamSynchronize(c.stream), "histogram copy");
+        std::vector<std::vector<std::pair<int64_t, uint64_t>>> rows((size_t)nthr);
+        for (size_t t = 0; t < (size_t)total; t++) {
+            const uint64_t key = pr[2 * t];
+            rows[(size_t)(key >> 40)].emplace_back((int64_t)(key & ((1ull << 40) - 1)),
+                                                   pr[2 * t + 1]);
+        }
+        for (int k = 0; k < nthr; k++) {
+            auto &r = rows[(size_t)k];
+            std::sort(r.begin(), r.end());
+            if (is_det) {
+                for (auto &b : r) b.second *= 2;
+                if (!r.empty() && r.back().first == nc) r.back().second += 1;
+                else r.emplace_back(nc, 1);
+            }
+            out.emplace_back(std::move(r), nc);
+        }
+        trace("fetch: %llu bins of %d thresholds wrapped", total, nthr);
+        return SUCCESS;
+    }
     std::vector<uint64_t> buf((size_t)p * nthr);
     CU(copy2d_d2h_async(buf.data(), (size_t)p * 8, d_hist, (size_t)stride * 8,
                         (size_t)p * 8, (size_t)nthr, c.stream),
        "cudaMemcpy(histogram D2H)");
     CU(cudaStreamSynchronize(c.stream), "histogram copy");
-    trace("fetch: %lld bins x %d thresholds copied", (long long)p, nthr);
-    out.clear();
-    out.reserve((size_t)nthr);
     for (int k = 0; k < nthr; k++) {
         std::vector<uint64_t> h(buf.begin() + (size_t)k * p, buf.begin() + (size_t)(k + 1) * p);
-        uint64_t last = 0;
-        if (kind == ACCRQA_WALK_DET) {
-            // Upper-triangle runs doubled, plus the line of identity
-            // (src/AccRQA_CPU_function.cpp:156-162).
+        if (is_det) {
             for (auto &v : h) v = 2 * v;
-            if (p == nc + 1) h[(size_t)nc] += 1;
-            else last = 1;
+            h[(size_t)nc] += 1;
         }
-        out.emplace_back(std::move(h), last, nc);
+        out.emplace_back(h, 0, nc);
     }
-    trace("fetch: histograms wrapped");
+    trace("fetch: dense rows of %d thresholds wrapped", nthr);
     return SUCCESS;
 }
 
@@ -724,7 +769,7 @@ Accrqa_Error run_lines_in(Context *c, int kind, T *out, const T *x, size_t n, co
             const int64_t nc = embedded_length(n, taus[a], embs[b]);
             std::vector<LineHistogram> hs;
             if ((err = fetch_histograms(*c, kind, d_hist + off[(size_t)(q - first)], nc + 1,
-                                        d_max + (size_t)(q - first) * nthr, nthr, nc, hs)))
+                                        nthr, nc, hs)))
                 return err;
             for (int k = 0; k < nthr; k++) {
                 const LineHistogram &h = hs[(size_t)k];

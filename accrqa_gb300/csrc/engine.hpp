@@ -45,6 +45,7 @@ struct Context {
     std::mutex mu;
     DeviceBuffer series, counts, hist, maxlen, rp[2];
     DeviceBuffer series_hi, series_lo;         // float split of a float64 series
+    DeviceBuffer pairs, pair_count;            // non-zero histogram bins fetched back
     std::vector<float> host_hi, host_lo;
     std::vector<uint64_t> host_u64;
     // batched path: side streams for concurrent launch groups, a device arena
@@ -107,13 +108,18 @@ Accrqa_Error enqueue_lines(int kind, const T *d_x, int64_t n, int tau, int emb,
                            double maxabs = 0.0);
 
 // ---- post-processing --------------------------------------------------------
-// A length histogram H[0..nc] held as a dense prefix H[0..P) plus the single
-// bin H[nc] (all bins between are zero).  The accessors return the
-// reference's metric[] and scan[] arrays (src/AccRQA_CPU_function.cpp:181-204)
-// with wrapping 64-bit arithmetic; indices past nc read 0.
+// A length histogram H[0..nc] held by its non-zero bins (ascending length).
+// The accessors return the reference's metric[] and scan[] arrays
+// (src/AccRQA_CPU_function.cpp:181-204) with wrapping 64-bit arithmetic;
+// indices past nc read 0.  Zero bins contribute nothing to any of the five
+// measures, and the entropy visits the non-zero bins in ascending length as
+// the reference's loop does, so the measures equal the dense computation's.
 class LineHistogram {
   public:
-    LineHistogram(std::vector<uint64_t> prefix, uint64_t h_last, int64_t nc);
+    // Dense prefix H[0..P) plus the single bin H[nc] (all bins between zero).
+    LineHistogram(const std::vector<uint64_t> &prefix, uint64_t h_last, int64_t nc);
+    // Non-zero bins (length, count), lengths strictly ascending, all <= nc.
+    LineHistogram(std::vector<std::pair<int64_t, uint64_t>> bins, int64_t nc);
     int64_t nc() const { return nc_; }
     uint64_t bin(int64_t l) const;
     uint64_t metric(int64_t l) const;
@@ -126,10 +132,11 @@ class LineHistogram {
     double rr() const;
 
   private:
-    std::vector<uint64_t> h_, m_, s_;   // prefix bins, suffix sums over the prefix
-    uint64_t h_last_ = 0;
+    void build_sums();
+    size_t first_at_least(int64_t l) const;   // first bin with length >= l
+    std::vector<int64_t> len_;
+    std::vector<uint64_t> cnt_, m_, s_;       // counts; suffix sums of l*H and H
     int64_t nc_ = 0;
-    int64_t p_ = 0;                     // prefix length, <= nc + 1
 };
 
 // ---- API-level drivers (reference semantics) -------------------------------

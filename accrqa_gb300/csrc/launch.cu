@@ -82,7 +82,52 @@ static cudaError_t launch_rp_bits_t(const void *d_x, int norm, long long nc, int
     return cudaGetLastError();
 }
 
+// Non-zero bins of nthr histogram rows (bins [0, p) at `stride`), one warp
+// per 32 bins: pairs[2t] = (row << 40) | length, pairs[2t+1] = count, slots
+// t reserved with one atomic per warp.  Slots at or past `cap` are counted
+// but not written (the caller then takes the dense rows instead).
+__global__ void compact_bins(const u64 *__restrict__ hist, long long stride, int nthr,
+                             long long p, u64 *__restrict__ pairs, long long cap,
+                             unsigned long long *__restrict__ count) {
+    const int lane = threadIdx.x & 31;
+    const long long gwarp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    const long long cpr = (p + 31) / 32;
+    for (long long c = gwarp; c < (long long)nthr * cpr; c += nwarps) {
+        const long long row = c / cpr;
+        const long long bin = (c - row * cpr) * 32 + lane;
+        const u64 v = bin < p ? hist[row * stride + bin] : 0ull;
+        const u32 nz = __ballot_sync(0xFFFFFFFFu, v != 0ull);
+        if (!nz) continue;
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(count, (unsigned long long)__popc(nz));
+        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        if (v) {
+            const long long t = (long long)base + __popc(nz & ((1u << lane) - 1u));
+            if (t < cap) {
+                pairs[2 * t] = ((u64)row << 40) | (u64)bin;
+                pairs[2 * t + 1] = v;
+            }
+        }
+    }
+}
+
 }  // namespace accrqa
+
+extern "C" int accrqa_gb300_launch_compact(const uint64_t *d_hist, int64_t stride, int32_t nthr,
+                                           int64_t p, uint64_t *d_pairs, int64_t cap,
+                                           unsigned long long *d_count, void *stream) {
+    using namespace accrqa;
+    if (nthr <= 0 || p <= 0) return (int)cudaSuccess;
+    const long long warps = (long long)nthr * ((p + 31) / 32);
+    long long blocks = (warps + 7) / 8;   // 8 warps of 256 threads
+    const long long cap_blocks = (long long)sm_count_cached() * 8;
+    if (blocks > cap_blocks) blocks = cap_blocks;
+    compact_bins<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(
+        (const u64 *)d_hist, stride, nthr, p, (u64 *)d_pairs, cap, d_count);
+    g_launches.fetch_add(1);
+    return (int)cudaGetLastError();
+}
 
 extern "C" int accrqa_gb300_launch_rp_bits(const void *d_x, int32_t dtype, int32_t norm,
                                            int64_t nc, int32_t tau, int32_t emb, uint64_t key,

@@ -239,11 +239,11 @@ template <> __device__ __forceinline__ double never_value<double>() { return __l
 constexpr int kGroup = 8;
 
 // float: four cell pairs.  d = v - lim on the f32x2 pipe, then one funnel
-// shift per cell moves its sign bit (recurrent) into the mask.  With STOP
-// (the LAM walker, where it measured faster) the warp checks every fourth
-// slot whether any lane still has a recurrent cell in the group and stops
-// pushing when none has.
-template <int NT, bool STOP = false>
+// shift per cell moves its sign bit (recurrent) into the mask.  With STOP > 0
+// the warp checks every STOP-th slot whether any lane still has a recurrent
+// cell in the group and stops pushing when none has; the interval that
+// measured best differs per walker (LAM 4, RR 8, DET none).
+template <int NT, int STOP = 0>
 __device__ __forceinline__ void push_group(u32 (&m)[NT], const f2 (&v)[kGroup / 2],
                                            const u64 (&keys)[kMaxThrPerPass]) {
     f2 d0[kGroup / 2];
@@ -275,7 +275,7 @@ __device__ __forceinline__ void push_group(u32 (&m)[NT], const f2 (&v)[kGroup / 
         }
         // every fourth slot: once no lane has a recurrent cell of the group
         // here, the narrower slots have none either (nested) -- shift zeros
-        if (STOP && (k & 3) == 0 &&
+        if (STOP > 0 && k % (STOP > 0 ? STOP : 1) == 0 &&
             !__any_sync(0xFFFFFFFFu, ((u32)anyk | (u32)(anyk >> 32)) >> 31)) {
 #pragma unroll
             for (int kk = k; kk < NT; kk++) m[kk] <<= kGroup;
@@ -290,7 +290,7 @@ __device__ __forceinline__ void push_group(u32 (&m)[NT], const f2 (&v)[kGroup / 
 }
 
 // double: an integer compare of the bit pattern against the limit.
-template <int NT, bool STOP = false>
+template <int NT, int STOP = 0>
 __device__ __forceinline__ void push_group(u32 (&m)[NT], const double (&v)[kGroup],
                                            const u64 (&keys)[kMaxThrPerPass]) {
     u64 lo = (u64)__double_as_longlong(v[0]);

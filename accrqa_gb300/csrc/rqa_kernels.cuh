@@ -330,7 +330,7 @@ __device__ __forceinline__ void exact_fixup(u32 (&m)[NT], u32 amb, const double 
 }
 
 // The masks of one 32-cell block of a row (cells xj[0..32)).
-template <typename T, int NORM, int EMB, int NT, bool CHECK, bool STOP = false>
+template <typename T, int NORM, int EMB, int NT, bool CHECK, int STOP = 0>
 __device__ __forceinline__ void row_masks(u32 (&m)[NT], const LaneVec<T, EMB> &a,
                                           typename SeriesOf<T>::ptr xi,
                                           typename SeriesOf<T>::ptr xj,
@@ -449,7 +449,7 @@ __device__ __forceinline__ void rr_block(const LaneVec<T, EMB> &a,
                                          const u64 (&keys)[kMaxThrPerPass], const u64 *xkeys,
                                          u32 (&up)[NT]) {
     u32 m[NT];
-    row_masks<T, NORM, EMB, NT, CHECK>(m, a, xi, xj, tau, emb, lo, hi, keys, xkeys);
+    row_masks<T, NORM, EMB, NT, CHECK, 8>(m, a, xi, xj, tau, emb, lo, hi, keys, xkeys);
 #pragma unroll
     for (int k = 0; k < NT; k++) up[k] += __popc(m[k]);
 }
@@ -585,7 +585,7 @@ __device__ __forceinline__ void lam_block(const LaneVec<T, EMB> &a,
                                           const u64 (&keys)[kMaxThrPerPass], const u64 *xkeys,
                                           u32 (&carry)[NT], const Sink &sink) {
     u32 m[NT];
-    row_masks<T, NORM, EMB, NT, CHECK, true>(m, a, xi, xj, tau, emb, 0, rem, keys, xkeys);
+    row_masks<T, NORM, EMB, NT, CHECK, 4>(m, a, xi, xj, tau, emb, 0, rem, keys, xkeys);
     close_block<NT, Sink>(m, carry, sink);
 }
 

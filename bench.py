@@ -397,12 +397,34 @@ def batched_section(args):
     log(f"plain: {t_plain:.3f} s")
     same = all(np.array_equal(o["rr"], r[0]) and np.array_equal(o["det"], r[1], equal_nan=True)
                and np.array_equal(o["lam"], r[2], equal_nan=True) for o, r in zip(outs, ref))
+
+    # per measure: each measure batched alone and as plain calls
+    per_measure = {}
+    one = cells // 3
+    for idx, meas in enumerate(("rr", "det", "lam")):
+        t0 = time.perf_counter()
+        engine.batch(jobs, measures=(meas,))
+        tb = time.perf_counter() - t0
+        fn = (A.RR, A.DET, A.LAM)[idx]
+        t0 = time.perf_counter()
+        for j in jobs:
+            D = A.accrqaDistance("euclidean" if j["norm"] == 1 else "maximal")
+            t = np.array([j["tau"]], np.intc)
+            e = np.array([j["emb"]], np.intc)
+            if meas == "rr":
+                fn(j["x"], t, e, j["thresholds"], D, tidy_data=False)
+            else:
+                fn(j["x"], t, e, np.array([2], np.intc), j["thresholds"], D, tidy_data=False)
+        tp = time.perf_counter() - t0
+        per_measure[meas] = {"batched_cells_per_s": one / tb, "plain_cells_per_s": one / tp,
+                             "speedup_vs_plain": tp / tb}
+    log("batched: per measure done")
     return {"workload": f"{len(jobs)} uneven series (1e3..6.4e4 log-uniform, mixed generators), "
                         "tau 1..4, emb 2..8, E/M norm, 8 thresholds, RR+DET+LAM, fp32",
             "value": cells / t_batch, "unit": "cells/s", "seconds": t_batch,
             "plain_value": cells / t_plain, "plain_seconds": t_plain,
             "speedup_vs_plain": t_plain / t_batch, "identical_results": bool(same),
-            "cells": cells}
+            "cells": cells, "per_measure": per_measure}
 
 
 # ---------------------------------------------------------------------------

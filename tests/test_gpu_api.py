@@ -233,3 +233,28 @@ def test_rp_bits_equal_byte_plot(gpu, dt):
             torch.cuda.synchronize()
             np.testing.assert_array_equal(dout.cpu().numpy().view(np.uint32).reshape(bits.shape),
                                           bits)
+
+
+def test_logistic_10k_workload(gpu, oracle_mod):
+    """The reference's CPU-runnable workload: logistic map N = 10,000 float32,
+    tau 1, emb 3, maximal norm, thresholds linspace(0.05, 0.40, 8), RR, DET
+    (lmin 2) and LAM (vmin 2) -- raw integers bit for bit, measures within
+    the float32 tolerance."""
+    from accrqa_gb300 import engine
+    x = workloads.logistic(10_000, 2024).astype(np.float32)
+    thr = np.linspace(0.05, 0.40, 8).astype(np.float32)
+    np.testing.assert_array_equal(engine.rr_counts(x, 1, 3, thr, 2),
+                                  oracle_mod.rr_counts(x, 1, 3, thr, 2))
+    det = engine.det_histograms(x, 1, 3, thr, 2)
+    lam = engine.lam_histograms(x, 1, 3, thr, 2)
+    for k, t in enumerate(thr):
+        np.testing.assert_array_equal(det[k], oracle_mod.det_hist(x, 1, 3, t, 2))
+        np.testing.assert_array_equal(lam[k], oracle_mod.lam_hist(x, 1, 3, t, 2))
+    one = np.array([1], np.intc)
+    three = np.array([3], np.intc)
+    lm = np.array([2], np.intc)
+    D = A.accrqaDistance("maximal")
+    _close(A.DET(x, one, three, lm, thr, D, tidy_data=False),
+           oracle_mod.line_output(x, [1], [3], lm, thr, 2, 1, True), np.float32)
+    _close(A.LAM(x, one, three, lm, thr, D, tidy_data=False),
+           oracle_mod.line_output(x, [1], [3], lm, thr, 2, 1, False), np.float32)

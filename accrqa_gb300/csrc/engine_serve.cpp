@@ -57,6 +57,10 @@ struct accrqa_gb300_server {
     std::vector<std::thread> workers;
     std::vector<accrqa::Context *> ctxs;
     uint64_t batches = 0, served = 0;
+    // At most one request larger than a quantum runs at a time: two of them
+    // side by side only stretch each other, while small batches still fill
+    // the GPU around one.
+    std::mutex big_mu;
 
     void work(int w) {
         using namespace accrqa;
@@ -87,7 +91,10 @@ struct accrqa_gb300_server {
             // A request taken alone goes through the per-series path (no
             // batch planning, graph or job tables to build for one series).
             Accrqa_Error e;
-            if (take.size() == 1) {
+            if (take.size() == 1 && take[0]->work > quantum) {
+                std::lock_guard<std::mutex> big(big_mu);
+                e = run_job_plain(*c, take[0]->job);
+            } else if (take.size() == 1) {
                 e = run_job_plain(*c, take[0]->job);
             } else {
                 std::vector<accrqa_gb300_series_job> jobs;

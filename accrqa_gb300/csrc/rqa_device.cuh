@@ -62,7 +62,8 @@ struct WalkArgs {
     long long hist_stride;
     u32 *maxlen;            // [nthr] longest line seen
     long long nbands;       // 32-line bands
-    long long nunits;       // work units (band pairs)
+    long long nunits;       // work units (band pairs; RR: band x chunk)
+    long long chunk;        // RR: 32-column blocks per unit
     // float64 series through the float filter (F64F kernels only): the
     // series split into float hi/lo parts, and the exact limits of the slots
     // (keys[] then hold the filter's float limit pairs)

@@ -439,7 +439,8 @@ struct LineSmem {
 
 // ---------------------------------------------------------------------------
 // RR: lane r of a warp owns row i = 32*band + r and walks the columns j >= i;
-// the main-diagonal cell (i, i) is counted once, the others twice.
+// the main-diagonal cell (i, i) is counted once, the others twice.  A unit is
+// one chunk of a band's columns.
 // ---------------------------------------------------------------------------
 template <typename T, int NORM, int EMB, int NT, bool CHECK>
 __device__ __forceinline__ void rr_block(const LaneVec<T, EMB> &a,
@@ -466,49 +467,58 @@ rr_rows(const __grid_constant__ WalkArgs p) {
     const long long nc = p.nc;
     const long long tau = p.tau;
 
-    // Lane k keeps the 64-bit total of slot k; per-band lane counters are
-    // 32-bit (a band walk adds at most nc per lane).
+    // Lane k keeps the 64-bit total of slot k; per-unit lane counters are
+    // 32-bit (a unit adds at most chunk*32 per lane).
     u64 total = 0;
+    // Units are (band, chunk of p.chunk 32-column blocks), chunk-major; a
+    // band's later chunks are empty once its columns run out.  Equal-size
+    // units keep every warp busy to the end of the pass.
+    const long long nbands = p.nbands, B = p.chunk;
 
     for (long long unit = gwarp; unit < p.nunits; unit += nwarps) {
-#pragma unroll 1
-        for (int half = 0; half < 2; half++) {
-            const long long band = half == 0 ? unit : p.nbands - 1 - unit;
-            if (half == 1 && band == unit) break;
-            const long long i = band * 32 + lane;
-            const bool row_ok = i < nc;
-            LaneVec<T, EMB> a;
-            a.load(x + i, tau);
-            u32 up[NT], dg[NT];
-            {
-                const auto v = cell_dist_mem<typename SeriesOf<T>::exact, NORM, EMB>(
-                    exact_ptr(x + i), exact_ptr(x + i), tau, p.emb);
+        const long long band = unit % nbands, chunk = unit / nbands;
+        const long long j0 = band * 32;
+        const long long nblk = (nc - j0 + 31) / 32;   // blocks of this band's row walk
+        long long kb = chunk * B;
+        if (kb >= nblk) continue;                     // warp-uniform
+        const long long ke = kb + B < nblk ? kb + B : nblk;
+        const long long i = j0 + lane;
+        const bool row_ok = i < nc;
+        LaneVec<T, EMB> a;
+        a.load(x + i, tau);
+        u32 up[NT], dg[NT];
 #pragma unroll
-                for (int k = 0; k < NT; k++) {
-                    dg[k] = (row_ok && is_rec_lim(v, xkeys[k])) ? 1u : 0u;
-                    up[k] = 0;
-                }
-            }
-            // first block: the columns j > i of the diagonal tile (j < nc)
-            const long long j0 = band * 32;
-            long long hi0 = nc - j0 < 32 ? nc - j0 : 32;
+        for (int k = 0; k < NT; k++) {
+            up[k] = 0;
+            dg[k] = 0;
+        }
+        if (kb == 0) {
+            // the main-diagonal cell, counted once, and the columns j > i of
+            // the diagonal tile (j < nc)
+            const auto v = cell_dist_mem<typename SeriesOf<T>::exact, NORM, EMB>(
+                exact_ptr(x + i), exact_ptr(x + i), tau, p.emb);
+#pragma unroll
+            for (int k = 0; k < NT; k++) dg[k] = (row_ok && is_rec_lim(v, xkeys[k])) ? 1u : 0u;
+            const long long hi0 = nc - j0 < 32 ? nc - j0 : 32;
             rr_block<T, NORM, EMB, NT, true>(a, x + i, x + j0, tau, p.emb, lane + 1, hi0, p.keys,
                                              xkeys, up);
-            // full blocks: j > i for every lane, all columns inside the matrix
-            long long jb = j0 + 32;
-            for (; jb + 32 <= nc; jb += 32)
-                rr_block<T, NORM, EMB, NT, false>(a, x + i, x + jb, tau, p.emb, 0, 32, p.keys, xkeys,
-                                                  up);
-            if (jb < nc)
-                rr_block<T, NORM, EMB, NT, true>(a, x + i, x + jb, tau, p.emb, 0, nc - jb, p.keys,
-                                                 xkeys, up);
+            kb = 1;
+        }
+        // full blocks: j > i for every lane, all columns inside the matrix
+        const long long kfull = (nc - j0) / 32 < ke ? (nc - j0) / 32 : ke;
+        long long k = kb;
+        for (; k < kfull; k++)
+            rr_block<T, NORM, EMB, NT, false>(a, x + i, x + j0 + 32 * k, tau, p.emb, 0, 32, p.keys,
+                                              xkeys, up);
+        if (k < ke)   // the row's last, partial block
+            rr_block<T, NORM, EMB, NT, true>(a, x + i, x + j0 + 32 * k, tau, p.emb, 0,
+                                             nc - j0 - 32 * k, p.keys, xkeys, up);
 #pragma unroll
-            for (int k = 0; k < NT; k++) {
-                u64 t = 2ull * (u64)(row_ok ? up[k] : 0u) + (u64)dg[k];
+        for (int s = 0; s < NT; s++) {
+            u64 t = 2ull * (u64)(row_ok ? up[s] : 0u) + (u64)dg[s];
 #pragma unroll
-                for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xFFFFFFFFu, t, o);
-                if (lane == k) total += t;
-            }
+            for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xFFFFFFFFu, t, o);
+            if (lane == s) total += t;
         }
     }
     if (lane < p.nthr && lane < NT && total) atomicAdd(&p.counts[p.row[lane]], total);

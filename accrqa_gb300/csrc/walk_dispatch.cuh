@@ -92,12 +92,20 @@ static cudaError_t launch_one(const accrqa_walk_desc &d, cudaStream_t st) {
         a.nbands = (d.nc + 31) / 32;
         a.nunits = a.nbands;
     } else if (KIND == ACCRQA_WALK_RR) {
+        // (band, chunk) units of equal size, about 8 per resident warp or more
         a.nbands = (d.nc + 31) / 32;
-        a.nunits = (a.nbands + 1) / 2;
+        const long long nblk0 = a.nbands;                        // blocks of band 0's walk
+        const long long total_blocks = a.nbands * (nblk0 + 1) / 2;
+        const long long resident = (long long)sm_count_cached() * per_sm * kWarpsPerCta;
+        long long B = total_blocks / (8 * resident);
+        B = B < 8 ? 8 : (B > 256 ? 256 : B);
+        a.chunk = B;
+        a.nunits = a.nbands * ((nblk0 + B - 1) / B);
     } else {
         a.nbands = (d.nc - 1 + 31) / 32;   // diagonals 1 .. nc-1
         a.nunits = (a.nbands + 1) / 2;
     }
+    if (KIND != ACCRQA_WALK_RR) a.chunk = 0;
     if (a.nunits <= 0) return cudaSuccess;
     long long want = (a.nunits + kWarpsPerCta - 1) / kWarpsPerCta;
     long long cap = (long long)sm_count_cached() * per_sm;

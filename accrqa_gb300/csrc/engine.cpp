@@ -12,6 +12,7 @@
 #include <cstring>
 #include <limits>
 #include <memory>
+#include <mutex>
 
 namespace accrqa {
 
@@ -354,6 +355,47 @@ Accrqa_Error enqueue_rr(const T *d_x, int64_t n, int tau, int emb, const T *thr,
     return SUCCESS;
 }
 
+// Stream-ordered scratch of the chunked line walks, from a private memory
+// pool per device that keeps its memory between passes (a pass allocates
+// and frees on its own stream, so passes on different streams never share
+// a buffer).  Null when the pool cannot serve it: the pass then walks its
+// lines whole.
+static void *line_scratch_alloc(size_t bytes, cudaStream_t st) {
+    static std::mutex mu;
+    static cudaMemPool_t pools[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    cudaMemPool_t pool;
+    {
+        std::lock_guard<std::mutex> g(mu);
+        if (!pools[dev]) {
+            cudaMemPoolProps props;
+            std::memset(&props, 0, sizeof(props));
+            props.allocType = cudaMemAllocationTypePinned;
+            props.location.type = cudaMemLocationTypeDevice;
+            props.location.id = dev;
+            cudaMemPool_t p = nullptr;
+            if (cudaMemPoolCreate(&p, &props) != cudaSuccess) {
+                cudaGetLastError();
+                return nullptr;
+            }
+            uint64_t keep = UINT64_MAX;
+            cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &keep);
+            pools[dev] = p;
+        }
+        pool = pools[dev];
+    }
+    void *ptr = nullptr;
+    if (cudaMallocFromPoolAsync(&ptr, bytes, pool, st) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return ptr;
+}
+
 template <typename T>
 Accrqa_Error enqueue_lines(int kind, const T *d_x, int64_t n, int tau, int emb,
                            const T *thr, int nthr, int norm, uint64_t *d_hist,
@@ -366,7 +408,11 @@ Accrqa_Error enqueue_lines(int kind, const T *d_x, int64_t n, int tau, int emb,
         d.d_hist = d_hist + (int64_t)k0 * stride;
         d.hist_stride = stride;
         d.d_maxlen = d_maxlen + k0;
+        const int64_t want = accrqa_gb300_walk_scratch_bytes(&d);
+        if (want > 0 && (d.d_scratch = line_scratch_alloc((size_t)want, st)) != nullptr)
+            d.scratch_bytes = want;
         int e = accrqa_gb300_launch_walk(&d, st);
+        if (d.d_scratch) cudaFreeAsync(d.d_scratch, st);
         if (e) return cuda_error((cudaError_t)e, kind == ACCRQA_WALK_DET ? "DET kernel launch" : "LAM kernel launch");
     }
     return SUCCESS;

@@ -62,11 +62,21 @@ typedef struct accrqa_walk_desc {
     const void *d_xhi;
     const void *d_xlo;
     uint64_t filter_keys[ACCRQA_MAX_THR_PER_PASS];
+    /* DET/LAM, optional: device scratch of accrqa_gb300_walk_scratch_bytes()
+     * bytes for the chunk boundary records; with it the lines are walked in
+     * equal chunks (a balanced grid) and joined by a second kernel on the
+     * same stream.  Without it (or too small) the lines are walked whole. */
+    void *d_scratch;
+    int64_t scratch_bytes;
 } accrqa_walk_desc;
 
 /* Enqueue one pass on `stream` (a cudaStream_t, 0 = legacy default stream).
  * Returns 0 or a cudaError_t value. */
 int accrqa_gb300_launch_walk(const accrqa_walk_desc *desc, void *stream);
+
+/* Scratch bytes the chunked walk of this pass wants (0: none, the lines go
+ * whole).  Reads kind, nc and nthr only. */
+int64_t accrqa_gb300_walk_scratch_bytes(const accrqa_walk_desc *desc);
 
 /* Enqueue the recurrence plot of rows [row0, row0 + nrows) into d_out
  * (row-major, nc columns; out_type 1 = int8, 2 = int32). */

@@ -142,6 +142,14 @@ extern "C" int accrqa_gb300_launch_rp_bits(const void *d_x, int32_t dtype, int32
     return (int)cudaErrorInvalidValue;
 }
 
+extern "C" int64_t accrqa_gb300_walk_scratch_bytes(const accrqa_walk_desc *d) {
+    using namespace accrqa;
+    if (!d || d->nc < 2 || (d->kind != ACCRQA_WALK_DET && d->kind != ACCRQA_WALK_LAM)) return 0;
+    const int nt = d->nthr <= 4 ? 4 : d->nthr <= 8 ? 8 : 16;   // slots of the instantiation
+    const LinePlan q = plan_lines(d->kind == ACCRQA_WALK_DET, d->nc, sm_count_cached(), true);
+    return (int64_t)q.nrecords * nt * 32 * 2 * (int64_t)sizeof(u32);
+}
+
 extern "C" int accrqa_gb300_sm_count(void) { return accrqa::sm_count_cached(); }
 
 extern "C" uint64_t accrqa_gb300_launch_count(void) { return accrqa::g_launches.load(); }

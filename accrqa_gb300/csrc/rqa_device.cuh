@@ -62,8 +62,15 @@ struct WalkArgs {
     long long hist_stride;
     u32 *maxlen;            // [nthr] longest line seen
     long long nbands;       // 32-line bands
-    long long nunits;       // work units (band pairs; RR: band x chunk)
-    long long chunk;        // RR: 32-column blocks per unit
+    long long nunits;       // work units (band pairs, or band x chunk)
+    long long chunk;        // 32-cell blocks per chunk (RR; chunked DET/LAM)
+    long long nchunks;      // chunks of the longest band (chunked DET/LAM)
+    // Chunked DET/LAM: per (band, chunk) record, slot and lane, the length of
+    // the run that opens the chunk (lead) and of the run still open at its
+    // end (trail; kRunSentinel + width when the whole chunk is recurrent).
+    // Null when the lines are walked whole.
+    u32 *lead;
+    u32 *trail;
     // float64 series through the float filter (F64F kernels only): the
     // series split into float hi/lo parts, and the exact limits of the slots
     // (keys[] then hold the filter's float limit pairs)
@@ -313,6 +320,11 @@ __device__ __forceinline__ void push_group(u32 (&m)[NT], const double (&v)[kGrou
     }
 }
 
+// A chunk of a line starts its open run at kRunSentinel, so the run that
+// opens the chunk -- whose true length depends on the chunks before it --
+// reaches the sink tagged (lengths stay below 2^31).
+constexpr u32 kRunSentinel = 0x80000000u;
+
 // ---------------------------------------------------------------------------
 // Line-length bookkeeping.  A block's mask holds 32 consecutive cells of one
 // line, the first cell of the block in bit 31 (the push order); `carry` is
@@ -324,10 +336,14 @@ struct HistSink {
     u64 *gh;          // global histogram base
     long long stride;
     const int *row;   // slot -> histogram row
+    u32 *lead;        // chunked walks: this lane's lead words, slot k at [32 k]
 
     __device__ __forceinline__ void emit(int k, u32 len) const {
         if (len < (u32)kShortRunBins) {
             atomicAdd(&sh[k * kShortRunBins + len], 1u);
+        } else if (len >= kRunSentinel) {
+            // the run that opened a chunk: its length goes to the stitch
+            lead[32 * k] = len - kRunSentinel;
         } else {
             atomicAdd(&gh[(long long)row[k] * stride + len], 1ull);
             atomicMax(&shmax[k], len);

@@ -32,10 +32,17 @@
 namespace accrqa {
 
 constexpr int kWarpsPerCta = 4;
-// Resident CTAs per SM the diagonal walker is compiled for (register cap, 80
-// registers): it waits on two loads per cell and dimension and needs the
-// warps to hide them.
-constexpr int kLineMinCtas = 6;
+// Resident CTAs per SM the line walkers are compiled for (register caps of
+// 96 and 72).  The diagonal walker waits on two loads per cell and dimension
+// and needs the warps to hide them; the row walker keeps its run state in
+// registers without spilling at 72.
+constexpr int kDiagMinCtas = 5;
+constexpr int kRowMinCtas = 7;
+// Work units per resident warp the chunked line walks aim at (0: the walk
+// never chunks).  Chunking DET evens out its unequal diagonals; LAM rows are
+// equal, and its grid only chunks when it would leave warps idle.
+constexpr int kDetUnitsPerWarp = 16;
+constexpr int kLamUnitsPerWarp = 16;
 constexpr int kSeriesPad = 128;
 
 // Distance of one cell with both operands read from memory (scalar path:
@@ -397,11 +404,32 @@ __device__ __forceinline__ void hist_smem_flush(const u32 *sh, const u32 *shmax,
         if (shmax[t]) atomicMax(&p.maxlen[p.row[t]], shmax[t]);
 }
 
-// Open-run lengths of every slot, one lane's line, in registers.
+// Open-run lengths of every slot, one lane's line, in registers (a chunk
+// of a line starts them at kRunSentinel).
 template <int NT>
-__device__ __forceinline__ void runs_begin(u32 (&carry)[NT]) {
+__device__ __forceinline__ void runs_begin(u32 (&carry)[NT], u32 init = 0u) {
 #pragma unroll
-    for (int k = 0; k < NT; k++) carry[k] = 0;
+    for (int k = 0; k < NT; k++) carry[k] = init;
+}
+
+// End of a chunk: the leads the sink kept in shared memory and the open runs
+// (trails) become the chunk's boundary record (the diagonal walker).  A slot whose chunk was all
+// recurrent has no lead; its trail says so and the stitch ignores the word.
+template <int NT>
+__device__ __forceinline__ void runs_store(const u32 (&carry)[NT], const u32 *lead_sh,
+                                           u32 *lead, u32 *trail) {
+#pragma unroll
+    for (int k = 0; k < NT; k++) {
+        lead[32 * k] = lead_sh[32 * k];
+        trail[32 * k] = carry[k];
+    }
+}
+
+// The same for a walker whose sink wrote the leads to global memory itself.
+template <int NT>
+__device__ __forceinline__ void runs_store(const u32 (&carry)[NT], u32 *trail) {
+#pragma unroll
+    for (int k = 0; k < NT; k++) trail[32 * k] = carry[k];
 }
 
 // Close the runs of one 32-cell block for every slot.  Slots nest (slot 0 is
@@ -430,12 +458,73 @@ __device__ __forceinline__ void runs_end(u32 (&carry)[NT], const Sink &sink) {
     }
 }
 
-// Shared memory of the line kernels: histogram bins and longest-run markers.
+// Shared memory of the line kernels: histogram bins, longest-run markers and
+// (chunked diagonal walks) the chunk leads of every warp's lanes
+// ([warp][slot][lane]).
 template <int NT>
 struct LineSmem {
-    static constexpr int kWords = NT * kShortRunBins + kMaxThrPerPass;
+    static constexpr int kLeadOffset = NT * kShortRunBins + kMaxThrPerPass;
+    static constexpr int kWords = kLeadOffset + kWarpsPerCta * NT * 32;
     static constexpr size_t kBytes = (size_t)kWords * sizeof(u32);
 };
+
+// ---------------------------------------------------------------------------
+// Chunked line walks.  A band is 32 lines -- LAM: rows 0..nc-1 of nc cells;
+// DET: diagonals 1..nc-1 -- walked in 32-cell blocks: every LAM band has
+// nbands blocks, DET band b has nbands - b.  Chunked, a unit is `chunk`
+// consecutive blocks of one band, numbered chunk-major (unit = c * nbands +
+// b; DET units past their band's end are empty), and each non-empty (band,
+// chunk) owns one boundary record of NT x 32 lead and trail words.  DET
+// records are packed by chunk: chunk c holds the bands b < nbands - c*chunk.
+// ---------------------------------------------------------------------------
+__host__ __device__ __forceinline__ long long line_band_blocks(bool det, long long nbands,
+                                                               long long b) {
+    return det ? nbands - b : nbands;
+}
+
+__host__ __device__ __forceinline__ long long line_record(bool det, long long nbands,
+                                                          long long chunk, long long c,
+                                                          long long b) {
+    return det ? c * nbands - chunk * (c * (c - 1) / 2) + b : c * nbands + b;
+}
+
+struct LinePlan {
+    long long nbands;    // 32-line bands
+    long long chunk;     // blocks per chunk (nbands when the lines go whole)
+    long long nchunks;   // chunks of the longest band (1 = whole lines)
+    long long nunits;    // units of the walk's grid-stride loop
+    long long nrecords;  // boundary records (0 = whole lines, no stitch)
+};
+
+// Chunks are sized for k{Det,Lam}UnitsPerWarp units per resident warp (at
+// most 8 CTAs of kWarpsPerCta warps per SM); a chunk spans at least 8
+// blocks, and a walk whose bands alone reach the target goes whole.  Whole
+// DET lines pair band b with band nbands-1-b (every pair walks about nc
+// cells per lane).
+inline LinePlan plan_lines(bool det, long long nc, int sms, bool allow_chunks) {
+    LinePlan q;
+    q.nbands = det ? (nc - 1 + 31) / 32 : (nc + 31) / 32;
+    const long long blocks = det ? q.nbands * (q.nbands + 1) / 2 : q.nbands * q.nbands;
+    const long long target = (long long)(det ? kDetUnitsPerWarp : kLamUnitsPerWarp) * sms * 8 *
+                             kWarpsPerCta;
+    long long B = target > 0 ? (blocks + target - 1) / target : q.nbands;
+    if (B < 8) B = 8;
+    long long K = q.nbands > 0 ? (q.nbands + B - 1) / B : 1;
+    if (!allow_chunks || K < 2 || B >= (1ll << 25)) {
+        q.chunk = q.nbands > 0 ? q.nbands : 1;
+        q.nchunks = 1;
+        q.nunits = det ? (q.nbands + 1) / 2 : q.nbands;
+        q.nrecords = 0;
+        return q;
+    }
+    B = (q.nbands + K - 1) / K;   // even chunks
+    K = (q.nbands + B - 1) / B;
+    q.chunk = B;
+    q.nchunks = K;
+    q.nunits = K * q.nbands;
+    q.nrecords = line_record(det, q.nbands, B, K, 0);
+    return q;
+}
 
 // ---------------------------------------------------------------------------
 // RR: lane r of a warp owns row i = 32*band + r and walks the columns j >= i;
@@ -542,14 +631,15 @@ __device__ __forceinline__ void det_block(typename SeriesOf<T>::ptr xs,
 }
 
 template <typename T, int NORM, int EMB, int NT>
-__global__ void __launch_bounds__(kWarpsPerCta * 32, kLineMinCtas)
+__global__ void __launch_bounds__(kWarpsPerCta * 32, kDiagMinCtas)
 det_diags(const __grid_constant__ WalkArgs p) {
     extern __shared__ u32 smem[];
     u32 *sh = smem;
     u32 *shmax = smem + NT * kShortRunBins;
     hist_smem_clear(sh, shmax, NT * kShortRunBins);
-    const HistSink sink{sh, shmax, p.hist, p.hist_stride, p.row};
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    u32 *lead_sh = smem + LineSmem<NT>::kLeadOffset + warp * NT * 32 + lane;
+    const HistSink sink{sh, shmax, p.hist, p.hist_stride, p.row, lead_sh};
     u32 carry[NT];
 
     const typename SeriesOf<T>::ptr x = series_ptr<T>(p);
@@ -558,34 +648,53 @@ det_diags(const __grid_constant__ WalkArgs p) {
     const long long nwarps = (long long)gridDim.x * kWarpsPerCta;
     const long long nc = p.nc;
     const long long tau = p.tau;
+    const bool chunked = p.lead != nullptr;
 
     for (long long unit = gwarp; unit < p.nunits; unit += nwarps) {
 #pragma unroll 1
         for (int half = 0; half < 2; half++) {
-            const long long band = half == 0 ? unit : p.nbands - 1 - unit;
-            if (half == 1 && band == unit) break;
+            // the unit's band and its blocks [kb, ke)
+            long long band, kb, ke;
+            if (chunked) {
+                if (half == 1) break;
+                band = unit % p.nbands;
+                const long long nb = p.nbands - band;
+                kb = (unit / p.nbands) * p.chunk;
+                if (kb >= nb) break;   // warp-uniform
+                ke = kb + p.chunk < nb ? kb + p.chunk : nb;
+            } else {
+                band = half == 0 ? unit : p.nbands - 1 - unit;
+                if (half == 1 && band == unit) break;
+                kb = 0;
+                ke = p.nbands - band;
+            }
             const long long d = 1 + band * 32 + lane;
             const long long len = nc - d;                 // cells on this diagonal
             const long long wmin = nc - (band * 32 + 32); // shortest diagonal of the warp
-            const long long wmax = nc - (band * 32 + 1);  // longest diagonal of the warp
-            runs_begin<NT>(carry);
-            long long s0 = 0;
-            for (; s0 + 32 <= wmin; s0 += 32)
+            runs_begin<NT>(carry, chunked ? kRunSentinel : 0u);
+            long long s0 = kb * 32;
+            const long long se = ke * 32;
+            for (; s0 + 32 <= wmin && s0 < se; s0 += 32)
                 det_block<T, NORM, EMB, NT, false>(x + s0, x + s0 + d, tau, p.emb, 32, p.keys, xkeys,
                                                    carry, sink);
-            for (; s0 < wmax; s0 += 32)
+            for (; s0 < se; s0 += 32)
                 det_block<T, NORM, EMB, NT, true>(x + s0, x + s0 + d, tau, p.emb, len - s0,
                                                   p.keys, xkeys, carry, sink);
-            runs_end<NT, HistSink>(carry, sink);
+            if (chunked) {
+                const long long rec =
+                    line_record(true, p.nbands, p.chunk, unit / p.nbands, band) * NT * 32 + lane;
+                runs_store<NT>(carry, lead_sh, p.lead + rec, p.trail + rec);
+            } else {
+                runs_end<NT, HistSink>(carry, sink);
+            }
         }
     }
     hist_smem_flush(sh, shmax, p);
 }
 
 // ---------------------------------------------------------------------------
-// LAM: lane r owns row i = 32*band + r of the full matrix and walks all
-// columns j = 0 .. nc-1, 32 at a time.  Every row has nc cells, so plain
-// band striding is balanced.
+// LAM: lane r owns row i = 32*band + r of the full matrix and walks its
+// columns j = 0 .. nc-1 (chunked: one chunk of them), 32 at a time.
 // ---------------------------------------------------------------------------
 template <typename T, int NORM, int EMB, int NT, bool CHECK, class Sink>
 __device__ __forceinline__ void lam_block(const LaneVec<T, EMB> &a,
@@ -600,14 +709,14 @@ __device__ __forceinline__ void lam_block(const LaneVec<T, EMB> &a,
 }
 
 template <typename T, int NORM, int EMB, int NT>
-__global__ void __launch_bounds__(kWarpsPerCta * 32)
+__global__ void __launch_bounds__(kWarpsPerCta * 32, kRowMinCtas)
 lam_rows(const __grid_constant__ WalkArgs p) {
     extern __shared__ u32 smem[];
     u32 *sh = smem;
     u32 *shmax = smem + NT * kShortRunBins;
     hist_smem_clear(sh, shmax, NT * kShortRunBins);
-    const HistSink sink{sh, shmax, p.hist, p.hist_stride, p.row};
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    HistSink sink{sh, shmax, p.hist, p.hist_stride, p.row, nullptr};
     u32 carry[NT];
 
     const typename SeriesOf<T>::ptr x = series_ptr<T>(p);
@@ -616,28 +725,81 @@ lam_rows(const __grid_constant__ WalkArgs p) {
     const long long nwarps = (long long)gridDim.x * kWarpsPerCta;
     const long long nc = p.nc;
     const long long tau = p.tau;
+    const bool chunked = p.lead != nullptr;
 
-    for (long long band = gwarp; band < p.nbands; band += nwarps) {
+    for (long long unit = gwarp; unit < p.nunits; unit += nwarps) {
+        // LAM records are (chunk, band) in unit order; leads go straight to
+        // global memory, so the row walker's shared memory stays at its bins
+        // (the rest of the carveout is L1 for the series stream)
+        if (chunked) sink.lead = p.lead + unit * NT * 32 + lane;
+        const long long band = chunked ? unit % p.nbands : unit;
+        // columns [jb, je) of this unit
+        const long long jb = chunked ? (unit / p.nbands) * p.chunk * 32 : 0;
+        const long long je = jb + p.chunk * 32 < nc ? jb + p.chunk * 32 : nc;
         const long long i = band * 32 + lane;
         const bool row_ok = i < nc;
         LaneVec<T, EMB> a;
         a.load(x + i, tau);
-        runs_begin<NT>(carry);
-        long long j0 = 0;
+        runs_begin<NT>(carry, chunked ? kRunSentinel : 0u);
+        long long j0 = jb;
         // All lanes walk together (the group decision is warp-wide); in the
         // last, partial band the rows past nc see only never-recurrent cells.
         if (band * 32 + 31 < nc) {
-            for (; j0 + 32 <= nc; j0 += 32)
+            for (; j0 + 32 <= je; j0 += 32)
                 lam_block<T, NORM, EMB, NT, false>(a, x + i, x + j0, tau, p.emb, 32, p.keys, xkeys, carry, sink);
-            if (j0 < nc)
+            if (j0 < je)
                 lam_block<T, NORM, EMB, NT, true>(a, x + i, x + j0, tau, p.emb, nc - j0, p.keys, xkeys, carry,
                                                   sink);
         } else {
-            for (; j0 < nc; j0 += 32)
+            for (; j0 < je; j0 += 32)
                 lam_block<T, NORM, EMB, NT, true>(a, x + i, x + j0, tau, p.emb,
                                                   row_ok ? nc - j0 : 0, p.keys, xkeys, carry, sink);
         }
-        runs_end<NT, HistSink>(carry, sink);
+        if (chunked) {
+            runs_store<NT>(carry, p.trail + unit * NT * 32 + lane);
+        } else {
+            runs_end<NT, HistSink>(carry, sink);
+        }
+    }
+    hist_smem_flush(sh, shmax, p);
+}
+
+// ---------------------------------------------------------------------------
+// Stitch of a chunked DET/LAM walk: one thread per (band, slot, lane) line
+// joins its chunks' boundary records in order -- a fully recurrent chunk
+// extends the pending run, any other closes it with its lead and opens its
+// trail -- and emits the runs that crossed chunk boundaries.
+// ---------------------------------------------------------------------------
+template <int NT>
+__global__ void __launch_bounds__(256)
+line_stitch(const __grid_constant__ WalkArgs p, int det) {
+    extern __shared__ u32 smem[];
+    u32 *sh = smem;
+    u32 *shmax = smem + NT * kShortRunBins;
+    hist_smem_clear(sh, shmax, NT * kShortRunBins);
+    const HistSink sink{sh, shmax, p.hist, p.hist_stride, p.row, nullptr};
+    const long long lines = p.nbands * NT * 32;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < lines;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int lane = (int)(t & 31);
+        const int k = (int)((t >> 5) % NT);
+        const long long b = (t >> 5) / NT;
+        if (k >= p.nthr) continue;
+        const long long nb = line_band_blocks(det != 0, p.nbands, b);
+        const long long kc = (nb + p.chunk - 1) / p.chunk;
+        u32 pending = 0;
+        for (long long c = 0; c < kc; c++) {
+            const long long r = line_record(det != 0, p.nbands, p.chunk, c, b) * NT * 32 + 32 * k + lane;
+            const u32 tr = p.trail[r];
+            if (tr >= kRunSentinel) {   // the whole chunk is recurrent
+                pending += tr - kRunSentinel;
+                continue;
+            }
+            pending += p.lead[r];
+            if (pending) sink.emit(k, pending);
+            pending = tr;
+        }
+        if (pending) sink.emit(k, pending);
     }
     hist_smem_flush(sh, shmax, p);
 }

@@ -23,14 +23,15 @@ template <int KIND, typename T, int NORM, int EMB, int NT>
 static cudaError_t launch_one(const accrqa_walk_desc &d, cudaStream_t st) {
     void (*kern)(WalkArgs);
     size_t smem = 0;
-    if (KIND == ACCRQA_WALK_RR) {
+    // if constexpr: a translation unit instantiates only its own kind
+    if constexpr (KIND == ACCRQA_WALK_RR) {
         kern = rr_rows<T, NORM, EMB, NT>;
-    } else if (KIND == ACCRQA_WALK_DET) {
+    } else if constexpr (KIND == ACCRQA_WALK_DET) {
         kern = det_diags<T, NORM, EMB, NT>;
         smem = LineSmem<NT>::kBytes;
     } else {
         kern = lam_rows<T, NORM, EMB, NT>;
-        smem = LineSmem<NT>::kBytes;
+        smem = (size_t)LineSmem<NT>::kLeadOffset * sizeof(u32);
     }
     // Resident CTAs per SM for this instantiation, computed once.
     static int per_sm = -1;
@@ -88,10 +89,26 @@ static cudaError_t launch_one(const accrqa_walk_desc &d, cudaStream_t st) {
     a.hist = (u64 *)d.d_hist;
     a.hist_stride = d.hist_stride;
     a.maxlen = d.d_maxlen;
-    if (KIND == ACCRQA_WALK_LAM) {
-        a.nbands = (d.nc + 31) / 32;
-        a.nunits = a.nbands;
-    } else if (KIND == ACCRQA_WALK_RR) {
+    a.lead = nullptr;
+    a.trail = nullptr;
+    a.nchunks = 1;
+    LinePlan q{};
+    if (KIND != ACCRQA_WALK_RR) {
+        // chunked when the caller's scratch holds the boundary records
+        const bool det = KIND == ACCRQA_WALK_DET;
+        q = plan_lines(det, d.nc, sm_count_cached(), d.d_scratch != nullptr);
+        const long long need = q.nrecords * NT * 32 * 2 * (long long)sizeof(u32);
+        if (q.nrecords > 0 && need > d.scratch_bytes)
+            q = plan_lines(det, d.nc, sm_count_cached(), false);
+        a.nbands = q.nbands;
+        a.nunits = q.nunits;
+        a.chunk = q.chunk;
+        a.nchunks = q.nchunks;
+        if (q.nrecords > 0) {
+            a.lead = (u32 *)d.d_scratch;
+            a.trail = a.lead + q.nrecords * NT * 32;
+        }
+    } else {
         // (band, chunk) units of equal size, about 8 per resident warp or more
         a.nbands = (d.nc + 31) / 32;
         const long long nblk0 = a.nbands;                        // blocks of band 0's walk
@@ -101,16 +118,26 @@ static cudaError_t launch_one(const accrqa_walk_desc &d, cudaStream_t st) {
         B = B < 8 ? 8 : (B > 256 ? 256 : B);
         a.chunk = B;
         a.nunits = a.nbands * ((nblk0 + B - 1) / B);
-    } else {
-        a.nbands = (d.nc - 1 + 31) / 32;   // diagonals 1 .. nc-1
-        a.nunits = (a.nbands + 1) / 2;
     }
-    if (KIND != ACCRQA_WALK_RR) a.chunk = 0;
     if (a.nunits <= 0) return cudaSuccess;
     long long want = (a.nunits + kWarpsPerCta - 1) / kWarpsPerCta;
     long long cap = (long long)sm_count_cached() * per_sm;
     int grid = (int)(want < cap ? want : cap);
+    // Only chunked diagonal walks keep leads in shared memory; the smaller
+    // shared-memory carveout leaves the rest to L1 (the series stream).
+    if (KIND == ACCRQA_WALK_LAM || q.nrecords == 0)
+        smem = (size_t)LineSmem<NT>::kLeadOffset * sizeof(u32);
     kern<<<grid, kWarpsPerCta * 32, smem, st>>>(a);
+    g_launches.fetch_add(1);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || q.nrecords == 0) return e;
+    // join the runs that cross chunk boundaries (same stream, after the walk)
+    const long long lines = q.nbands * NT * 32;
+    long long sgrid = (lines + 255) / 256;
+    const long long scap = (long long)sm_count_cached() * 8;
+    if (sgrid > scap) sgrid = scap;
+    line_stitch<NT><<<(unsigned)sgrid, 256, LineSmem<NT>::kBytes, st>>>(
+        a, KIND == ACCRQA_WALK_DET ? 1 : 0);
     g_launches.fetch_add(1);
     return cudaGetLastError();
 }

@@ -1,0 +1,86 @@
+"""GPU: chunked line walks equal whole-line walks, bit for bit.
+
+The DET/LAM kernels split lines into equal chunks when the caller gives
+scratch for the chunk boundary records, and join the runs that cross chunk
+boundaries in a second kernel.  Here the same pass is enqueued through the
+kernel library's C ABI (accrqa_gb300_launch_walk) with and without scratch,
+and the histograms and longest-line markers must be identical -- with a
+threshold that makes every cell recurrent (every chunk full, one run per
+line), one that makes almost none recurrent, and a spread between.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from accrqa_gb300 import _lib, engine, workloads
+
+pytestmark = pytest.mark.gpu
+
+MAX_THR = 16
+WALK_DET, WALK_LAM = 1, 2
+
+
+class WalkDesc(ctypes.Structure):
+    """accrqa_walk_desc of accrqa_gb300/csrc/engine_abi.h."""
+    _fields_ = [
+        ("kind", ctypes.c_int32), ("dtype", ctypes.c_int32), ("norm", ctypes.c_int32),
+        ("tau", ctypes.c_int32), ("emb", ctypes.c_int32), ("nthr", ctypes.c_int32),
+        ("nc", ctypes.c_int64), ("d_x", ctypes.c_void_p),
+        ("keys", ctypes.c_uint64 * MAX_THR),
+        ("d_counts", ctypes.c_void_p), ("d_hist", ctypes.c_void_p),
+        ("hist_stride", ctypes.c_int64), ("d_maxlen", ctypes.c_void_p),
+        ("d_xhi", ctypes.c_void_p), ("d_xlo", ctypes.c_void_p),
+        ("filter_keys", ctypes.c_uint64 * MAX_THR),
+        ("d_scratch", ctypes.c_void_p), ("scratch_bytes", ctypes.c_int64),
+    ]
+
+
+def _walk(torch, lib, kind, dx, dt, n, tau, emb, thr, norm, chunked):
+    nc = n - (emb - 1) * tau
+    keys = engine.threshold_keys(thr, dt, norm)
+    hist = torch.zeros((len(thr), nc + 1), dtype=torch.int64, device="cuda")
+    mx = torch.zeros(MAX_THR, dtype=torch.int32, device="cuda")
+    d = WalkDesc()
+    d.kind, d.dtype, d.norm = kind, engine.F32 if dt == np.float32 else engine.F64, norm
+    d.tau, d.emb, d.nthr, d.nc = tau, emb, len(thr), nc
+    d.d_x = dx.data_ptr()
+    for k in range(len(thr)):
+        d.keys[k] = int(keys[k])
+    d.d_hist, d.hist_stride, d.d_maxlen = hist.data_ptr(), nc + 1, mx.data_ptr()
+    scratch = None
+    if chunked:
+        want = lib.accrqa_gb300_walk_scratch_bytes(ctypes.byref(d))
+        assert want > 0, "this size must chunk"
+        scratch = torch.empty(want, dtype=torch.uint8, device="cuda")
+        d.d_scratch, d.scratch_bytes = scratch.data_ptr(), want
+    st = torch.cuda.current_stream().cuda_stream
+    assert lib.accrqa_gb300_launch_walk(ctypes.byref(d), ctypes.c_void_p(st)) == 0
+    torch.cuda.synchronize()
+    return hist.cpu().numpy(), mx.cpu().numpy()[:len(thr)]
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+@pytest.mark.parametrize("kind", [WALK_DET, WALK_LAM])
+@pytest.mark.parametrize("n,tau,emb,norm", [(20000, 1, 3, 1), (9000, 2, 5, 2), (3001, 1, 1, 1)])
+def test_chunked_equals_whole(kind, dt, n, tau, emb, norm):
+    torch = pytest.importorskip("torch")
+    lib = _lib.handle()
+    lib.accrqa_gb300_walk_scratch_bytes.restype = ctypes.c_int64
+    lib.accrqa_gb300_walk_scratch_bytes.argtypes = [ctypes.c_void_p]
+    lib.accrqa_gb300_launch_walk.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    x = workloads.logistic(n, 7 + n).astype(dt)
+    # 0: exact matches only; 4.0: beyond the largest distance (all recurrent)
+    thr = np.array([0.0, 0.01, 0.05, 0.1, 0.2, 0.3, 0.5, 0.8, 1.2, 4.0], dtype=dt)
+    dx = torch.zeros(n + 128, dtype=torch.float32 if dt == np.float32 else torch.float64,
+                     device="cuda")
+    dx[:n] = torch.from_numpy(x).cuda()
+    h0, m0 = _walk(torch, lib, kind, dx, dt, n, tau, emb, thr, norm, chunked=False)
+    h1, m1 = _walk(torch, lib, kind, dx, dt, n, tau, emb, thr, norm, chunked=True)
+    np.testing.assert_array_equal(h1, h0)
+    np.testing.assert_array_equal(m1, m0)
+    nc = n - (emb - 1) * tau
+    if kind == WALK_LAM:
+        assert h0[-1, nc] == nc          # every row one run of nc cells
+    else:
+        assert h0[-1, 1:].sum() == nc - 1  # every strict-upper diagonal one run

@@ -143,6 +143,40 @@ __device__ __forceinline__ void row_group(f2 (&v)[kGroup / 2], const LaneVec<flo
         v[q] = r;
     }
 }
+// Per-warp staging of a row block's partner values (float series, fixed
+// embedding): lane c copies xj[c + m*tau] to stage[32 m + c] for every m, so
+// each cell pair of the block reads its operand pair as one 64-bit shared
+// load instead of two scalar broadcast loads through L1.
+template <typename T, int EMB> struct RowStage {
+    static constexpr bool kOn = false;
+    static constexpr int kWords = 1;
+};
+template <int EMB> struct RowStage<float, EMB> {
+    static constexpr bool kOn = EMB > 0;
+    static constexpr int kWords = EMB > 0 ? EMB * 32 : 1;
+};
+
+template <int NORM, int EMB, bool CHECK>
+__device__ __forceinline__ void row_group_staged(f2 (&v)[kGroup / 2],
+                                                 const LaneVec<float, EMB> &a,
+                                                 const float *stage, int g, long long lo,
+                                                 long long hi) {
+#pragma unroll
+    for (int q = 0; q < kGroup / 2; q++) {
+        Dist2<NORM> d{0.0f, 0.0f};
+#pragma unroll
+        for (int m = 0; m < EMB; m++)
+            d.step(a.v[m], *reinterpret_cast<const f2 *>(stage + 32 * m + g + 2 * q), m == 0);
+        f2 r = d.value();
+        if (CHECK) {
+            const int c = g + 2 * q;
+            const bool ok0 = in_range(c, lo, hi), ok1 = in_range(c + 1, lo, hi);
+            r = pack2(ok0 ? lo_of(r) : never_value<float>(), ok1 ? hi_of(r) : never_value<float>());
+        }
+        v[q] = r;
+    }
+}
+
 template <int NORM, int EMB, bool CHECK>
 __device__ __forceinline__ void row_group(double (&v)[kGroup], const LaneVec<double, EMB> &a,
                                           const double *__restrict__ xi,
@@ -342,13 +376,30 @@ __device__ __forceinline__ void row_masks(u32 (&m)[NT], const LaneVec<T, EMB> &a
                                           typename SeriesOf<T>::ptr xi,
                                           typename SeriesOf<T>::ptr xj,
                                           long long tau, int emb, long long lo, long long hi,
-                                          const u64 (&keys)[kMaxThrPerPass], const u64 *xkeys) {
+                                          const u64 (&keys)[kMaxThrPerPass], const u64 *xkeys,
+                                          float *stage) {
 #pragma unroll
     for (int k = 0; k < NT; k++) m[k] = 0;
+    if constexpr (RowStage<T, EMB>::kOn) {
+        if (stage) {
+            const int lane = threadIdx.x & 31;
+            __syncwarp();   // the previous block's reads are done
+#pragma unroll
+            for (int d = 0; d < EMB; d++) stage[32 * d + lane] = __ldg(xj + lane + d * tau);
+            __syncwarp();
+        }
+    }
 #pragma unroll 1
     for (int g = 0; g < 32; g += kGroup) {
         typename GroupOf<T>::type v;
-        row_group<NORM, EMB, CHECK>(v, a, xi, xj, tau, emb, g, lo, hi);
+        if constexpr (RowStage<T, EMB>::kOn) {
+            if (stage)
+                row_group_staged<NORM, EMB, CHECK>(v, a, stage, g, lo, hi);
+            else
+                row_group<NORM, EMB, CHECK>(v, a, xi, xj, tau, emb, g, lo, hi);
+        } else {
+            row_group<NORM, EMB, CHECK>(v, a, xi, xj, tau, emb, g, lo, hi);
+        }
         if constexpr (std::is_same<T, F64F>::value) {
             const u32 amb = push_group_filtered<NT>(m, v, keys);
             if (__any_sync(0xFFFFFFFFu, amb != 0u))
@@ -537,9 +588,9 @@ __device__ __forceinline__ void rr_block(const LaneVec<T, EMB> &a,
                                          typename SeriesOf<T>::ptr xj,
                                          long long tau, int emb, long long lo, long long hi,
                                          const u64 (&keys)[kMaxThrPerPass], const u64 *xkeys,
-                                         u32 (&up)[NT]) {
+                                         u32 (&up)[NT], float *stage = nullptr) {
     u32 m[NT];
-    row_masks<T, NORM, EMB, NT, CHECK, 8>(m, a, xi, xj, tau, emb, lo, hi, keys, xkeys);
+    row_masks<T, NORM, EMB, NT, CHECK, 8>(m, a, xi, xj, tau, emb, lo, hi, keys, xkeys, stage);
 #pragma unroll
     for (int k = 0; k < NT; k++) up[k] += __popc(m[k]);
 }
@@ -547,6 +598,9 @@ __device__ __forceinline__ void rr_block(const LaneVec<T, EMB> &a,
 template <typename T, int NORM, int EMB, int NT>
 __global__ void __launch_bounds__(kWarpsPerCta * 32)
 rr_rows(const __grid_constant__ WalkArgs p) {
+    __shared__ __align__(16) float stage_cta[kWarpsPerCta * RowStage<T, EMB>::kWords];
+    float *stage = RowStage<T, EMB>::kOn ? stage_cta + (threadIdx.x >> 5) * RowStage<T, EMB>::kWords
+                                         : nullptr;
     const typename SeriesOf<T>::ptr x = series_ptr<T>(p);
     // exact limits: the float filter of float64 keeps them apart from keys[]
     const u64 *xkeys = std::is_same<T, F64F>::value ? p.xkeys : p.keys;
@@ -590,7 +644,7 @@ rr_rows(const __grid_constant__ WalkArgs p) {
             for (int k = 0; k < NT; k++) dg[k] = (row_ok && is_rec_lim(v, xkeys[k])) ? 1u : 0u;
             const long long hi0 = nc - j0 < 32 ? nc - j0 : 32;
             rr_block<T, NORM, EMB, NT, true>(a, x + i, x + j0, tau, p.emb, lane + 1, hi0, p.keys,
-                                             xkeys, up);
+                                             xkeys, up, stage);
             kb = 1;
         }
         // full blocks: j > i for every lane, all columns inside the matrix
@@ -598,10 +652,10 @@ rr_rows(const __grid_constant__ WalkArgs p) {
         long long k = kb;
         for (; k < kfull; k++)
             rr_block<T, NORM, EMB, NT, false>(a, x + i, x + j0 + 32 * k, tau, p.emb, 0, 32, p.keys,
-                                              xkeys, up);
+                                              xkeys, up, stage);
         if (k < ke)   // the row's last, partial block
             rr_block<T, NORM, EMB, NT, true>(a, x + i, x + j0 + 32 * k, tau, p.emb, 0,
-                                             nc - j0 - 32 * k, p.keys, xkeys, up);
+                                             nc - j0 - 32 * k, p.keys, xkeys, up, stage);
 #pragma unroll
         for (int s = 0; s < NT; s++) {
             u64 t = 2ull * (u64)(row_ok ? up[s] : 0u) + (u64)dg[s];
@@ -702,9 +756,10 @@ __device__ __forceinline__ void lam_block(const LaneVec<T, EMB> &a,
                                           typename SeriesOf<T>::ptr xj,
                                           long long tau, int emb, long long rem,
                                           const u64 (&keys)[kMaxThrPerPass], const u64 *xkeys,
-                                          u32 (&carry)[NT], const Sink &sink) {
+                                          u32 (&carry)[NT], const Sink &sink,
+                                          float *stage = nullptr) {
     u32 m[NT];
-    row_masks<T, NORM, EMB, NT, CHECK, 4>(m, a, xi, xj, tau, emb, 0, rem, keys, xkeys);
+    row_masks<T, NORM, EMB, NT, CHECK, 4>(m, a, xi, xj, tau, emb, 0, rem, keys, xkeys, stage);
     close_block<NT, Sink>(m, carry, sink);
 }
 
@@ -712,10 +767,12 @@ template <typename T, int NORM, int EMB, int NT>
 __global__ void __launch_bounds__(kWarpsPerCta * 32, kRowMinCtas)
 lam_rows(const __grid_constant__ WalkArgs p) {
     extern __shared__ u32 smem[];
+    __shared__ __align__(16) float stage_cta[kWarpsPerCta * RowStage<T, EMB>::kWords];
     u32 *sh = smem;
     u32 *shmax = smem + NT * kShortRunBins;
     hist_smem_clear(sh, shmax, NT * kShortRunBins);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float *stage = RowStage<T, EMB>::kOn ? stage_cta + warp * RowStage<T, EMB>::kWords : nullptr;
     HistSink sink{sh, shmax, p.hist, p.hist_stride, p.row, nullptr};
     u32 carry[NT];
 
@@ -746,14 +803,14 @@ lam_rows(const __grid_constant__ WalkArgs p) {
         // last, partial band the rows past nc see only never-recurrent cells.
         if (band * 32 + 31 < nc) {
             for (; j0 + 32 <= je; j0 += 32)
-                lam_block<T, NORM, EMB, NT, false>(a, x + i, x + j0, tau, p.emb, 32, p.keys, xkeys, carry, sink);
+                lam_block<T, NORM, EMB, NT, false>(a, x + i, x + j0, tau, p.emb, 32, p.keys, xkeys, carry, sink, stage);
             if (j0 < je)
                 lam_block<T, NORM, EMB, NT, true>(a, x + i, x + j0, tau, p.emb, nc - j0, p.keys, xkeys, carry,
-                                                  sink);
+                                                  sink, stage);
         } else {
             for (; j0 < je; j0 += 32)
                 lam_block<T, NORM, EMB, NT, true>(a, x + i, x + j0, tau, p.emb,
-                                                  row_ok ? nc - j0 : 0, p.keys, xkeys, carry, sink);
+                                                  row_ok ? nc - j0 : 0, p.keys, xkeys, carry, sink, stage);
         }
         if (chunked) {
             runs_store<NT>(carry, p.trail + unit * NT * 32 + lane);

@@ -222,6 +222,61 @@ __device__ __forceinline__ void diag_group(f2 (&v)[kGroup / 2], const float *__r
         v[q] = r;
     }
 }
+// Per-warp staging of a diagonal block (float series, fixed embedding).  For
+// dimension m the warp's cells read xs[c + m*tau] (the same for every lane)
+// and xsd[c + m*tau] = w[lane + c + m*tau], w the window that starts at lane
+// 0's diagonal.  Staged: A[m][c] = xs[c + m*tau] (32 floats) and B[m][k] =
+// the pair (w[k + m*tau], w[k + 1 + m*tau]) for k < 64, so every cell pair
+// reads both operand pairs with one 64-bit shared load each.
+template <typename T, int EMB> struct DiagStage {
+    static constexpr bool kOn = false;
+    static constexpr int kWords = 1;
+};
+template <int EMB> struct DiagStage<float, EMB> {
+    static constexpr bool kOn = EMB > 0;
+    static constexpr int kWords = EMB > 0 ? EMB * (32 + 2 * 64) : 1;
+};
+
+template <int EMB>
+__device__ __forceinline__ void diag_stage(float *stage, const float *__restrict__ xs,
+                                           const float *__restrict__ xsd, long long tau) {
+    const int lane = threadIdx.x & 31;
+    const int up = (lane + 1) & 31;
+    const float *w = xsd - lane;
+    f2 *b = reinterpret_cast<f2 *>(stage + EMB * 32);
+    __syncwarp();   // the previous block's reads are done
+#pragma unroll
+    for (int m = 0; m < EMB; m++) {
+        stage[32 * m + lane] = __ldg(xs + lane + m * tau);
+        const float v0 = __ldg(w + lane + m * tau), v1 = __ldg(w + 32 + lane + m * tau);
+        const float t0 = __shfl_sync(0xFFFFFFFFu, v0, up);   // w[k + 1], lanes < 31
+        const float t1 = __shfl_sync(0xFFFFFFFFu, v1, up);   // w[32 + k + 1]; lane 31: w[32]
+        b[64 * m + lane] = pack2(v0, lane < 31 ? t0 : t1);
+        b[64 * m + 32 + lane] = pack2(v1, t1);   // k = 63 is never read
+    }
+    __syncwarp();
+}
+
+template <int NORM, int EMB, bool CHECK>
+__device__ __forceinline__ void diag_group_staged(f2 (&v)[kGroup / 2], const float *stage, int g,
+                                                  long long rem) {
+    const int lane = threadIdx.x & 31;
+    const f2 *b = reinterpret_cast<const f2 *>(stage + EMB * 32);
+#pragma unroll
+    for (int q = 0; q < kGroup / 2; q++) {
+        const int c = g + 2 * q;
+        Dist2<NORM> d{0.0f, 0.0f};
+#pragma unroll
+        for (int m = 0; m < EMB; m++)
+            d.step(*reinterpret_cast<const f2 *>(stage + 32 * m + c), b[64 * m + lane + c], m == 0);
+        f2 r = d.value();
+        if (CHECK)
+            r = pack2((long long)c < rem ? lo_of(r) : never_value<float>(),
+                      (long long)c + 1 < rem ? hi_of(r) : never_value<float>());
+        v[q] = r;
+    }
+}
+
 template <int NORM, int EMB, bool CHECK>
 __device__ __forceinline__ void diag_group(double (&v)[kGroup], const double *__restrict__ xs,
                                            const double *__restrict__ xsd, long long tau,
@@ -416,13 +471,23 @@ template <typename T, int NORM, int EMB, int NT, bool CHECK>
 __device__ __forceinline__ void diag_masks(u32 (&m)[NT], typename SeriesOf<T>::ptr xs,
                                            typename SeriesOf<T>::ptr xsd, long long tau, int emb,
                                            long long rem, const u64 (&keys)[kMaxThrPerPass],
-                                           const u64 *xkeys) {
+                                           const u64 *xkeys, float *stage) {
 #pragma unroll
     for (int k = 0; k < NT; k++) m[k] = 0;
+    if constexpr (DiagStage<T, EMB>::kOn) {
+        if (stage) diag_stage<EMB>(stage, xs, xsd, tau);
+    }
 #pragma unroll 1
     for (int g = 0; g < 32; g += kGroup) {
         typename GroupOf<T>::type v;
-        diag_group<NORM, EMB, CHECK>(v, xs, xsd, tau, emb, g, rem);
+        if constexpr (DiagStage<T, EMB>::kOn) {
+            if (stage)
+                diag_group_staged<NORM, EMB, CHECK>(v, stage, g, rem);
+            else
+                diag_group<NORM, EMB, CHECK>(v, xs, xsd, tau, emb, g, rem);
+        } else {
+            diag_group<NORM, EMB, CHECK>(v, xs, xsd, tau, emb, g, rem);
+        }
         if constexpr (std::is_same<T, F64F>::value) {
             const u32 amb = push_group_filtered<NT>(m, v, keys);
             if (__any_sync(0xFFFFFFFFu, amb != 0u))
@@ -463,20 +528,9 @@ __device__ __forceinline__ void runs_begin(u32 (&carry)[NT], u32 init = 0u) {
     for (int k = 0; k < NT; k++) carry[k] = init;
 }
 
-// End of a chunk: the leads the sink kept in shared memory and the open runs
-// (trails) become the chunk's boundary record (the diagonal walker).  A slot whose chunk was all
-// recurrent has no lead; its trail says so and the stitch ignores the word.
-template <int NT>
-__device__ __forceinline__ void runs_store(const u32 (&carry)[NT], const u32 *lead_sh,
-                                           u32 *lead, u32 *trail) {
-#pragma unroll
-    for (int k = 0; k < NT; k++) {
-        lead[32 * k] = lead_sh[32 * k];
-        trail[32 * k] = carry[k];
-    }
-}
-
-// The same for a walker whose sink wrote the leads to global memory itself.
+// End of a chunk: the open runs become the chunk's trail records (the sink
+// wrote the leads as they closed).  A slot whose chunk was all recurrent has
+// no lead; its trail says so and the stitch ignores the lead word.
 template <int NT>
 __device__ __forceinline__ void runs_store(const u32 (&carry)[NT], u32 *trail) {
 #pragma unroll
@@ -509,13 +563,10 @@ __device__ __forceinline__ void runs_end(u32 (&carry)[NT], const Sink &sink) {
     }
 }
 
-// Shared memory of the line kernels: histogram bins, longest-run markers and
-// (chunked diagonal walks) the chunk leads of every warp's lanes
-// ([warp][slot][lane]).
+// Shared memory of the line kernels: histogram bins and longest-run markers.
 template <int NT>
 struct LineSmem {
-    static constexpr int kLeadOffset = NT * kShortRunBins + kMaxThrPerPass;
-    static constexpr int kWords = kLeadOffset + kWarpsPerCta * NT * 32;
+    static constexpr int kWords = NT * kShortRunBins + kMaxThrPerPass;
     static constexpr size_t kBytes = (size_t)kWords * sizeof(u32);
 };
 
@@ -678,9 +729,10 @@ __device__ __forceinline__ void det_block(typename SeriesOf<T>::ptr xs,
                                           typename SeriesOf<T>::ptr xsd,
                                           long long tau, int emb, long long rem,
                                           const u64 (&keys)[kMaxThrPerPass], const u64 *xkeys,
-                                          u32 (&carry)[NT], const Sink &sink) {
+                                          u32 (&carry)[NT], const Sink &sink,
+                                          float *stage = nullptr) {
     u32 m[NT];
-    diag_masks<T, NORM, EMB, NT, CHECK>(m, xs, xsd, tau, emb, rem, keys, xkeys);
+    diag_masks<T, NORM, EMB, NT, CHECK>(m, xs, xsd, tau, emb, rem, keys, xkeys, stage);
     close_block<NT, Sink>(m, carry, sink);
 }
 
@@ -688,12 +740,13 @@ template <typename T, int NORM, int EMB, int NT>
 __global__ void __launch_bounds__(kWarpsPerCta * 32, kDiagMinCtas)
 det_diags(const __grid_constant__ WalkArgs p) {
     extern __shared__ u32 smem[];
+    __shared__ __align__(16) float stage_cta[kWarpsPerCta * DiagStage<T, EMB>::kWords];
     u32 *sh = smem;
     u32 *shmax = smem + NT * kShortRunBins;
     hist_smem_clear(sh, shmax, NT * kShortRunBins);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    u32 *lead_sh = smem + LineSmem<NT>::kLeadOffset + warp * NT * 32 + lane;
-    const HistSink sink{sh, shmax, p.hist, p.hist_stride, p.row, lead_sh};
+    float *stage = DiagStage<T, EMB>::kOn ? stage_cta + warp * DiagStage<T, EMB>::kWords : nullptr;
+    HistSink sink{sh, shmax, p.hist, p.hist_stride, p.row, nullptr};
     u32 carry[NT];
 
     const typename SeriesOf<T>::ptr x = series_ptr<T>(p);
@@ -713,9 +766,12 @@ det_diags(const __grid_constant__ WalkArgs p) {
                 if (half == 1) break;
                 band = unit % p.nbands;
                 const long long nb = p.nbands - band;
-                kb = (unit / p.nbands) * p.chunk;
+                const long long c = unit / p.nbands;
+                kb = c * p.chunk;
                 if (kb >= nb) break;   // warp-uniform
                 ke = kb + p.chunk < nb ? kb + p.chunk : nb;
+                // leads go straight to global memory (see the stitch)
+                sink.lead = p.lead + line_record(true, p.nbands, p.chunk, c, band) * NT * 32 + lane;
             } else {
                 band = half == 0 ? unit : p.nbands - 1 - unit;
                 if (half == 1 && band == unit) break;
@@ -730,14 +786,12 @@ det_diags(const __grid_constant__ WalkArgs p) {
             const long long se = ke * 32;
             for (; s0 + 32 <= wmin && s0 < se; s0 += 32)
                 det_block<T, NORM, EMB, NT, false>(x + s0, x + s0 + d, tau, p.emb, 32, p.keys, xkeys,
-                                                   carry, sink);
+                                                   carry, sink, stage);
             for (; s0 < se; s0 += 32)
                 det_block<T, NORM, EMB, NT, true>(x + s0, x + s0 + d, tau, p.emb, len - s0,
-                                                  p.keys, xkeys, carry, sink);
+                                                  p.keys, xkeys, carry, sink, stage);
             if (chunked) {
-                const long long rec =
-                    line_record(true, p.nbands, p.chunk, unit / p.nbands, band) * NT * 32 + lane;
-                runs_store<NT>(carry, lead_sh, p.lead + rec, p.trail + rec);
+                runs_store<NT>(carry, p.trail + (sink.lead - p.lead));
             } else {
                 runs_end<NT, HistSink>(carry, sink);
             }

@@ -31,7 +31,7 @@ static cudaError_t launch_one(const accrqa_walk_desc &d, cudaStream_t st) {
         smem = LineSmem<NT>::kBytes;
     } else {
         kern = lam_rows<T, NORM, EMB, NT>;
-        smem = (size_t)LineSmem<NT>::kLeadOffset * sizeof(u32);
+        smem = LineSmem<NT>::kBytes;
     }
     // Resident CTAs per SM for this instantiation, computed once.
     static int per_sm = -1;
@@ -123,10 +123,6 @@ static cudaError_t launch_one(const accrqa_walk_desc &d, cudaStream_t st) {
     long long want = (a.nunits + kWarpsPerCta - 1) / kWarpsPerCta;
     long long cap = (long long)sm_count_cached() * per_sm;
     int grid = (int)(want < cap ? want : cap);
-    // Only chunked diagonal walks keep leads in shared memory; the smaller
-    // shared-memory carveout leaves the rest to L1 (the series stream).
-    if (KIND == ACCRQA_WALK_LAM || q.nrecords == 0)
-        smem = (size_t)LineSmem<NT>::kLeadOffset * sizeof(u32);
     kern<<<grid, kWarpsPerCta * 32, smem, st>>>(a);
     g_launches.fetch_add(1);
     cudaError_t e = cudaGetLastError();

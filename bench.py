@@ -65,10 +65,12 @@ def cells_per_step(measures=3):
 
 # DRAM bytes (read + write) per launch of the dominant kernel, lam_rows, on
 # this workload: the mean over the 12 launches of one step in an ncu capture
-# (dram__bytes_read.sum + dram__bytes_write.sum).  The kernel reads the series
-# (0.8 MB, L2-resident) and writes histograms with atomics, so this stays far
-# below what the FP32 side could move.
-LAM_TRAFFIC_PER_LAUNCH = 1_582_059
+# (dram__bytes_read.sum + dram__bytes_write.sum).  Reads are the series (0.8
+# MB, L2-resident) and its re-reads, 8.6 MB; writes are the chunk boundary
+# records (13 chunks x 6250 bands x 16 slots x 32 lanes x lead and trail,
+# 333 MB, partly still in L2 at the end), 282 MB.  About 4.7 GB/s beside 11
+# TFLOP/s of algorithmic FP32 work: HBM is not the bound.
+LAM_TRAFFIC_PER_LAUNCH = 290_648_747
 
 
 def algo_ops(nc, emb, nthr):

@@ -23,8 +23,11 @@ static cudaError_t batch_one(const accrqa_batch_launch &L, cudaStream_t st, int 
     const size_t smem = BatchSmem<NT>::kBytes;
     static int per_sm = -1;
     if (per_sm < 0) {
-        if (smem > 48 * 1024)
-            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        // the bins are dynamic, the operand stage static: together they can
+        // pass the 48 KB that a kernel gets without opting in
+        cudaError_t ea = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)smem);
+        if (ea != cudaSuccess) return ea;
         int v = 0;
         cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kern, kWarpsPerCta * 32, smem);
         if (e != cudaSuccess) return e;

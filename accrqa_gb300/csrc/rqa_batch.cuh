@@ -82,12 +82,21 @@ struct WarpSink {
     }
 };
 
+// At least 4 CTAs per SM (at most 128 registers): the staged diagonal walk
+// would otherwise take 168 at 16 slots and emb 8.
 template <int KIND, typename T, int NORM, int EMB, int NT>
-__global__ void __launch_bounds__(kWarpsPerCta * 32)
+__global__ void __launch_bounds__(kWarpsPerCta * 32, 4)
 batch_walk(const BatchJob *__restrict__ jobs, const BatchUnit *__restrict__ units,
            const int *__restrict__ warp_begin, int nwarps_total) {
     extern __shared__ u32 smem[];
+    // operand staging of the block walkers (float series, fixed embedding)
+    constexpr bool kStageOn =
+        KIND == ACCRQA_WALK_DET ? DiagStage<T, EMB>::kOn : RowStage<T, EMB>::kOn;
+    constexpr int kStageWords =
+        KIND == ACCRQA_WALK_DET ? DiagStage<T, EMB>::kWords : RowStage<T, EMB>::kWords;
+    __shared__ __align__(16) float stage_cta[kWarpsPerCta * kStageWords];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float *stage = kStageOn ? stage_cta + warp * kStageWords : nullptr;
     u32 *wbase = smem + warp * BatchSmem<NT>::kWarpWords;
     u32 *bins = wbase;
     u32 *bmax = bins + NT * kBatchBins;
@@ -137,14 +146,14 @@ batch_walk(const BatchJob *__restrict__ jobs, const BatchUnit *__restrict__ unit
             long long j0 = 0;
             if (band * 32 + 31 < nc) {
                 for (; j0 + 32 <= nc; j0 += 32)
-                    lam_block<T, NORM, EMB, NT, false>(a, x + i, x + j0, tau, emb, 32, keys, xkeys, carry, sink);
+                    lam_block<T, NORM, EMB, NT, false>(a, x + i, x + j0, tau, emb, 32, keys, xkeys, carry, sink, stage);
                 if (j0 < nc)
                     lam_block<T, NORM, EMB, NT, true>(a, x + i, x + j0, tau, emb, nc - j0, keys, xkeys, carry,
-                                                      sink);
+                                                      sink, stage);
             } else {
                 for (; j0 < nc; j0 += 32)
                     lam_block<T, NORM, EMB, NT, true>(a, x + i, x + j0, tau, emb,
-                                                      row_ok ? nc - j0 : 0, keys, xkeys, carry, sink);
+                                                      row_ok ? nc - j0 : 0, keys, xkeys, carry, sink, stage);
             }
             runs_end<NT, WarpSink>(carry, sink);
         } else {
@@ -162,10 +171,10 @@ batch_walk(const BatchJob *__restrict__ jobs, const BatchUnit *__restrict__ unit
                     long long s0 = 0;
                     for (; s0 + 32 <= wmin; s0 += 32)
                         det_block<T, NORM, EMB, NT, false>(x + s0, x + s0 + d, tau, emb, 32, keys,
-                                                           xkeys, carry, sink);
+                                                           xkeys, carry, sink, stage);
                     for (; s0 < wmax; s0 += 32)
                         det_block<T, NORM, EMB, NT, true>(x + s0, x + s0 + d, tau, emb, len - s0,
-                                                          keys, xkeys, carry, sink);
+                                                          keys, xkeys, carry, sink, stage);
                     runs_end<NT, WarpSink>(carry, sink);
                 } else {
                     const long long i = band * 32 + lane;
@@ -185,14 +194,14 @@ batch_walk(const BatchJob *__restrict__ jobs, const BatchUnit *__restrict__ unit
                     const long long j0 = band * 32;
                     const long long hi0 = nc - j0 < 32 ? nc - j0 : 32;
                     rr_block<T, NORM, EMB, NT, true>(a, x + i, x + j0, tau, emb, lane + 1, hi0, keys,
-                                                     xkeys, up);
+                                                     xkeys, up, stage);
                     long long jb = j0 + 32;
                     for (; jb + 32 <= nc; jb += 32)
                         rr_block<T, NORM, EMB, NT, false>(a, x + i, x + jb, tau, emb, 0, 32, keys,
-                                                          xkeys, up);
+                                                          xkeys, up, stage);
                     if (jb < nc)
                         rr_block<T, NORM, EMB, NT, true>(a, x + i, x + jb, tau, emb, 0, nc - jb, keys,
-                                                         xkeys, up);
+                                                         xkeys, up, stage);
 #pragma unroll
                     for (int k = 0; k < NT; k++) {
                         u64 t = 2ull * (u64)(row_ok ? up[k] : 0u) + (u64)dg[k];

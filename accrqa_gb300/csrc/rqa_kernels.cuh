@@ -38,6 +38,17 @@ constexpr int kWarpsPerCta = 4;
 // registers without spilling at 72.
 constexpr int kDiagMinCtas = 5;
 constexpr int kRowMinCtas = 7;
+// The float filter of float64 keeps hi and lo parts of the lane's vector
+// (4 x emb registers): its row walkers run at 4 CTAs per SM (128 registers).
+// The RR walker keeps per-slot counters instead of run state: 5 CTAs (96
+// registers) up to emb 3, 4 above.
+constexpr int kWideMinCtas = 4;
+template <typename T> constexpr int row_min_ctas() {
+    return std::is_same<T, F64F>::value ? kWideMinCtas : kRowMinCtas;
+}
+template <typename T, int EMB> constexpr int rr_min_ctas() {
+    return !std::is_same<T, F64F>::value && EMB > 0 && EMB <= 3 ? 5 : kWideMinCtas;
+}
 // Work units per resident warp the chunked line walks aim at (0: the walk
 // never chunks).  Chunking DET evens out its unequal diagonals; LAM rows are
 // equal, and its grid only chunks when it would leave warps idle.
@@ -143,17 +154,37 @@ __device__ __forceinline__ void row_group(f2 (&v)[kGroup / 2], const LaneVec<flo
         v[q] = r;
     }
 }
-// Per-warp staging of a row block's partner values (float series, fixed
-// embedding): lane c copies xj[c + m*tau] to stage[32 m + c] for every m, so
-// each cell pair of the block reads its operand pair as one 64-bit shared
-// load instead of two scalar broadcast loads through L1.
+// Per-warp staging of a row block's partner values (fixed embedding): lane c
+// copies xj[c + m*tau] to stage[32 m + c] for every m (the float filter of
+// float64: hi parts at [64 m + c], lo parts at [64 m + 32 + c]), so each cell
+// pair of the block reads its operand pair as one 64-bit shared load instead
+// of two scalar broadcast loads through L1.
 template <typename T, int EMB> struct RowStage {
     static constexpr bool kOn = false;
     static constexpr int kWords = 1;
+    static __device__ __forceinline__ void load(float *, typename SeriesOf<T>::ptr, long long) {}
 };
 template <int EMB> struct RowStage<float, EMB> {
     static constexpr bool kOn = EMB > 0;
     static constexpr int kWords = EMB > 0 ? EMB * 32 : 1;
+    static __device__ __forceinline__ void load(float *stage, const float *__restrict__ xj,
+                                                long long tau) {
+        const int lane = threadIdx.x & 31;
+#pragma unroll
+        for (int m = 0; m < EMB; m++) stage[32 * m + lane] = __ldg(xj + lane + m * tau);
+    }
+};
+template <int EMB> struct RowStage<F64F, EMB> {
+    static constexpr bool kOn = EMB > 0;
+    static constexpr int kWords = EMB > 0 ? EMB * 64 : 1;
+    static __device__ __forceinline__ void load(float *stage, F64FPtr xj, long long tau) {
+        const int lane = threadIdx.x & 31;
+#pragma unroll
+        for (int m = 0; m < EMB; m++) {
+            stage[64 * m + lane] = __ldg(xj.h + lane + m * tau);
+            stage[64 * m + 32 + lane] = __ldg(xj.l + lane + m * tau);
+        }
+    }
 };
 
 template <int NORM, int EMB, bool CHECK>
@@ -343,6 +374,27 @@ __device__ __forceinline__ void row_group(f2 (&v)[kGroup / 2], const LaneVec<F64
 }
 
 template <int NORM, int EMB, bool CHECK>
+__device__ __forceinline__ void row_group_staged(f2 (&v)[kGroup / 2],
+                                                 const LaneVec<F64F, EMB> &a,
+                                                 const float *stage, int g, long long lo,
+                                                 long long hi) {
+#pragma unroll
+    for (int q = 0; q < kGroup / 2; q++) {
+        const int c = g + 2 * q;
+        DistF2<NORM> d{0, 0.0f, 0.0f};
+#pragma unroll
+        for (int m = 0; m < EMB; m++)
+            d.step(a.h[m], a.l[m], *reinterpret_cast<const f2 *>(stage + 64 * m + c),
+                   *reinterpret_cast<const f2 *>(stage + 64 * m + 32 + c), m == 0);
+        f2 r = d.value();
+        if (CHECK)
+            r = pack2(in_range(c, lo, hi) ? lo_of(r) : never_value<float>(),
+                      in_range(c + 1, lo, hi) ? hi_of(r) : never_value<float>());
+        v[q] = r;
+    }
+}
+
+template <int NORM, int EMB, bool CHECK>
 __device__ __forceinline__ void diag_group(f2 (&v)[kGroup / 2], F64FPtr xs, F64FPtr xsd,
                                            long long tau, int emb, int g, long long rem) {
 #pragma unroll
@@ -437,10 +489,8 @@ __device__ __forceinline__ void row_masks(u32 (&m)[NT], const LaneVec<T, EMB> &a
     for (int k = 0; k < NT; k++) m[k] = 0;
     if constexpr (RowStage<T, EMB>::kOn) {
         if (stage) {
-            const int lane = threadIdx.x & 31;
             __syncwarp();   // the previous block's reads are done
-#pragma unroll
-            for (int d = 0; d < EMB; d++) stage[32 * d + lane] = __ldg(xj + lane + d * tau);
+            RowStage<T, EMB>::load(stage, xj, tau);
             __syncwarp();
         }
     }
@@ -647,7 +697,7 @@ __device__ __forceinline__ void rr_block(const LaneVec<T, EMB> &a,
 }
 
 template <typename T, int NORM, int EMB, int NT>
-__global__ void __launch_bounds__(kWarpsPerCta * 32)
+__global__ void __launch_bounds__(kWarpsPerCta * 32, rr_min_ctas<T, EMB>())
 rr_rows(const __grid_constant__ WalkArgs p) {
     __shared__ __align__(16) float stage_cta[kWarpsPerCta * RowStage<T, EMB>::kWords];
     float *stage = RowStage<T, EMB>::kOn ? stage_cta + (threadIdx.x >> 5) * RowStage<T, EMB>::kWords
@@ -818,7 +868,7 @@ __device__ __forceinline__ void lam_block(const LaneVec<T, EMB> &a,
 }
 
 template <typename T, int NORM, int EMB, int NT>
-__global__ void __launch_bounds__(kWarpsPerCta * 32, kRowMinCtas)
+__global__ void __launch_bounds__(kWarpsPerCta * 32, row_min_ctas<T>())
 lam_rows(const __grid_constant__ WalkArgs p) {
     extern __shared__ u32 smem[];
     __shared__ __align__(16) float stage_cta[kWarpsPerCta * RowStage<T, EMB>::kWords];

@@ -82,18 +82,28 @@ struct WarpSink {
     }
 };
 
-// At least 4 CTAs per SM (at most 128 registers): the staged diagonal walk
-// would otherwise take 168 at 16 slots and emb 8.
+// At least 4 CTAs per SM (at most 128 registers) for float series: the
+// staged diagonal walk would otherwise take 168 at 16 slots and emb 8.
+// float64 (plain or through the float filter) keeps 3 (168 registers).
+template <typename T> constexpr int batch_min_ctas() {
+    return std::is_same<T, float>::value ? 4 : 3;
+}
+
 template <int KIND, typename T, int NORM, int EMB, int NT>
-__global__ void __launch_bounds__(kWarpsPerCta * 32, 4)
+__global__ void __launch_bounds__(kWarpsPerCta * 32, batch_min_ctas<T>())
 batch_walk(const BatchJob *__restrict__ jobs, const BatchUnit *__restrict__ units,
            const int *__restrict__ warp_begin, int nwarps_total) {
     extern __shared__ u32 smem[];
-    // operand staging of the block walkers (float series, fixed embedding)
-    constexpr bool kStageOn =
-        KIND == ACCRQA_WALK_DET ? DiagStage<T, EMB>::kOn : RowStage<T, EMB>::kOn;
-    constexpr int kStageWords =
-        KIND == ACCRQA_WALK_DET ? DiagStage<T, EMB>::kWords : RowStage<T, EMB>::kWords;
+    // operand staging of the block walkers (float series, fixed embedding);
+    // the float filter's stages beside the per-warp bins would cost registers
+    // or a CTA per SM
+    constexpr bool kFloat = std::is_same<T, float>::value;
+    constexpr bool kStageOn = !kFloat ? false
+                              : KIND == ACCRQA_WALK_DET ? DiagStage<T, EMB>::kOn
+                                                        : RowStage<T, EMB>::kOn;
+    constexpr int kStageWords = !kFloat ? 1
+                                : KIND == ACCRQA_WALK_DET ? DiagStage<T, EMB>::kWords
+                                                          : RowStage<T, EMB>::kWords;
     __shared__ __align__(16) float stage_cta[kWarpsPerCta * kStageWords];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     float *stage = kStageOn ? stage_cta + warp * kStageWords : nullptr;

@@ -267,6 +267,13 @@ template <int EMB> struct DiagStage<float, EMB> {
     static constexpr bool kOn = EMB > 0;
     static constexpr int kWords = EMB > 0 ? EMB * (32 + 2 * 64) : 1;
 };
+// The float filter of float64: per dimension the hi and lo parts of A (32
+// floats each, read as pairs) and of the window (64 floats each, read as two
+// scalar loads: pre-pairing both would not fit five CTAs per SM).
+template <int EMB> struct DiagStage<F64F, EMB> {
+    static constexpr bool kOn = EMB > 0;
+    static constexpr int kWords = EMB > 0 ? EMB * 192 : 1;
+};
 
 template <int EMB>
 __device__ __forceinline__ void diag_stage(float *stage, const float *__restrict__ xs,
@@ -516,6 +523,50 @@ __device__ __forceinline__ void row_masks(u32 (&m)[NT], const LaneVec<T, EMB> &a
     }
 }
 
+// Staged float filter diagonals (DiagStage<F64F>).
+template <int EMB>
+__device__ __forceinline__ void diag_stage_f64f(float *stage, F64FPtr xs, F64FPtr xsd,
+                                                long long tau) {
+    const int lane = threadIdx.x & 31;
+    const float *wh = xsd.h - lane, *wl = xsd.l - lane;
+    __syncwarp();   // the previous block's reads are done
+#pragma unroll
+    for (int m = 0; m < EMB; m++) {
+        float *s = stage + 192 * m;
+        const long long o = lane + m * tau;
+        s[lane] = __ldg(xs.h + o);
+        s[32 + lane] = __ldg(xs.l + o);
+        s[64 + lane] = __ldg(wh + o);
+        s[96 + lane] = __ldg(wh + 32 + o);
+        s[128 + lane] = __ldg(wl + o);
+        s[160 + lane] = __ldg(wl + 32 + o);
+    }
+    __syncwarp();
+}
+
+template <int NORM, int EMB, bool CHECK>
+__device__ __forceinline__ void diag_group_staged_f64f(f2 (&v)[kGroup / 2], const float *stage,
+                                                       int g, long long rem) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int q = 0; q < kGroup / 2; q++) {
+        const int c = g + 2 * q;
+        DistF2<NORM> d{0, 0.0f, 0.0f};
+#pragma unroll
+        for (int m = 0; m < EMB; m++) {
+            const float *s = stage + 192 * m;
+            const int w = lane + c;
+            d.step(*reinterpret_cast<const f2 *>(s + c), *reinterpret_cast<const f2 *>(s + 32 + c),
+                   pack2(s[64 + w], s[64 + w + 1]), pack2(s[128 + w], s[128 + w + 1]), m == 0);
+        }
+        f2 r = d.value();
+        if (CHECK)
+            r = pack2((long long)c < rem ? lo_of(r) : never_value<float>(),
+                      (long long)c + 1 < rem ? hi_of(r) : never_value<float>());
+        v[q] = r;
+    }
+}
+
 // The masks of one 32-cell block of a diagonal (cells (xs[c], xsd[c])).
 template <typename T, int NORM, int EMB, int NT, bool CHECK>
 __device__ __forceinline__ void diag_masks(u32 (&m)[NT], typename SeriesOf<T>::ptr xs,
@@ -525,16 +576,25 @@ __device__ __forceinline__ void diag_masks(u32 (&m)[NT], typename SeriesOf<T>::p
 #pragma unroll
     for (int k = 0; k < NT; k++) m[k] = 0;
     if constexpr (DiagStage<T, EMB>::kOn) {
-        if (stage) diag_stage<EMB>(stage, xs, xsd, tau);
+        if (stage) {
+            if constexpr (std::is_same<T, F64F>::value)
+                diag_stage_f64f<EMB>(stage, xs, xsd, tau);
+            else
+                diag_stage<EMB>(stage, xs, xsd, tau);
+        }
     }
 #pragma unroll 1
     for (int g = 0; g < 32; g += kGroup) {
         typename GroupOf<T>::type v;
         if constexpr (DiagStage<T, EMB>::kOn) {
-            if (stage)
-                diag_group_staged<NORM, EMB, CHECK>(v, stage, g, rem);
-            else
+            if (stage) {
+                if constexpr (std::is_same<T, F64F>::value)
+                    diag_group_staged_f64f<NORM, EMB, CHECK>(v, stage, g, rem);
+                else
+                    diag_group_staged<NORM, EMB, CHECK>(v, stage, g, rem);
+            } else {
                 diag_group<NORM, EMB, CHECK>(v, xs, xsd, tau, emb, g, rem);
+            }
         } else {
             diag_group<NORM, EMB, CHECK>(v, xs, xsd, tau, emb, g, rem);
         }

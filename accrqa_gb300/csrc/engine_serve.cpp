@@ -136,8 +136,10 @@ Server *accrqa_gb300_server_create(int32_t workers, double hbm_fraction) {
         free_b = (size_t)8 << 30;
     }
     s->budget = (size_t)((double)free_b * hbm_fraction / workers);
-    // about 10 ms of float32 work on a GB300 (~1e13 cell-thresholds per second)
-    s->quantum = 1.0e11;
+    // about 1 ms of float32 work on a GB300 (~1.7e13 cell-thresholds per
+    // second): a request in a batch completes when the whole batch does, and
+    // one series already fills the GPU, so batches stay short
+    s->quantum = 2.0e10;
     for (int w = 0; w < workers; w++) {
         Context *c = context_create(&err);
         if (!c) return nullptr;

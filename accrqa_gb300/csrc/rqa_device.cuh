@@ -64,7 +64,6 @@ struct WalkArgs {
     long long nbands;       // 32-line bands
     long long nunits;       // work units (band pairs, or band x chunk)
     long long chunk;        // 32-cell blocks per chunk (RR; chunked DET/LAM)
-    long long nchunks;      // chunks of the longest band (chunked DET/LAM)
     // Chunked DET/LAM: per (band, chunk) record, slot and lane, the length of
     // the run that opens the chunk (lead) and of the run still open at its
     // end (trail; kRunSentinel + width when the whole chunk is recurrent).

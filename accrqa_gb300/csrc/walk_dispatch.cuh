@@ -91,7 +91,6 @@ static cudaError_t launch_one(const accrqa_walk_desc &d, cudaStream_t st) {
     a.maxlen = d.d_maxlen;
     a.lead = nullptr;
     a.trail = nullptr;
-    a.nchunks = 1;
     LinePlan q{};
     if (KIND != ACCRQA_WALK_RR) {
         // chunked when the caller's scratch holds the boundary records
@@ -103,7 +102,6 @@ static cudaError_t launch_one(const accrqa_walk_desc &d, cudaStream_t st) {
         a.nbands = q.nbands;
         a.nunits = q.nunits;
         a.chunk = q.chunk;
-        a.nchunks = q.nchunks;
         if (q.nrecords > 0) {
             a.lead = (u32 *)d.d_scratch;
             a.trail = a.lead + q.nrecords * NT * 32;

@@ -21,7 +21,10 @@ template <int KIND, typename T, int NORM, int EMB, int NT>
 static cudaError_t batch_one(const accrqa_batch_launch &L, cudaStream_t st, int *warps_out) {
     auto kern = batch_walk<KIND, T, NORM, EMB, NT>;
     const size_t smem = BatchSmem<NT>::kBytes;
-    static int per_sm = -1;
+    // computed once; the attribute is set before the value is published, so
+    // a thread that sees the value launches after it
+    static std::atomic<int> per_sm_cache{-1};
+    int per_sm = per_sm_cache.load();
     if (per_sm < 0) {
         // the bins are dynamic, the operand stage static: together they can
         // pass the 48 KB that a kernel gets without opting in
@@ -32,6 +35,7 @@ static cudaError_t batch_one(const accrqa_batch_launch &L, cudaStream_t st, int 
         cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kern, kWarpsPerCta * 32, smem);
         if (e != cudaSuccess) return e;
         per_sm = v > 0 ? v : 1;
+        per_sm_cache.store(per_sm);
     }
     if (warps_out) {
         *warps_out = sm_count_cached() * per_sm * kWarpsPerCta;

@@ -33,14 +33,17 @@ static cudaError_t launch_one(const accrqa_walk_desc &d, cudaStream_t st) {
         kern = lam_rows<T, NORM, EMB, NT>;
         smem = LineSmem<NT>::kBytes;
     }
-    // Resident CTAs per SM for this instantiation, computed once.
-    static int per_sm = -1;
+    // Resident CTAs per SM for this instantiation, computed once (threads
+    // that race on the first call compute the same value).
+    static std::atomic<int> per_sm_cache{-1};
+    int per_sm = per_sm_cache.load();
     if (per_sm < 0) {
         int v = 0;
         cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
             &v, kern, kWarpsPerCta * 32, smem);
         if (e != cudaSuccess) return e;
         per_sm = v > 0 ? v : 1;
+        per_sm_cache.store(per_sm);
     }
     WalkArgs a;
     a.x = d.d_x;

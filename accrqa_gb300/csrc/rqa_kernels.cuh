@@ -1,7 +1,7 @@
 // rqa_kernels.cuh -- the hot kernels of the GB300 RQA engine.
 //
 //   rr_rows   : recurrent-cell counts per threshold (RR), upper triangle by
-//               rows, one warp per 32-row band; replaces
+//               rows, one warp per 32-row band and column chunk; replaces
 //               GPU_RQA_RR_seedsSM_improved_reduction_kernel
 //               (src/AccRQA-GPU-RR.cu:61-121).
 //   det_diags : diagonal-line histograms per threshold (DET), one lane per
@@ -12,15 +12,18 @@
 //               row of the full matrix (the matrix is symmetric, rows and
 //               columns give the same histogram); replaces
 //               GPU_RQA_HST_length_histogram_vertical (src/AccRQA-GPU-HST.cu:401-438).
+//   line_stitch: joins the runs that cross the chunk boundaries of a
+//               chunked DET/LAM walk.
 //   rp_cells  : the recurrence plot itself (the reference computes it on the
 //               CPU only, src/AccRQA_CPU_function.cpp:226-244).
 //
 // All thresholds of a pass (up to 16) are decided from one distance
-// evaluation.  Lines are tracked as 32-bit masks per lane and threshold;
-// runs crossing mask boundaries are carried in registers along the line, so
-// no second pass or inter-block exchange is needed.  Work units pair band b
-// with band nbands-1-b so that every warp walks the same number of cells;
-// grids are persistent and warps stride over units.
+// evaluation, on operands each warp stages per 32-cell block in shared
+// memory.  Lines are tracked as 32-bit masks per lane and threshold; runs
+// crossing mask boundaries are carried in registers along the line.  Work
+// units are equal chunks of a band's lines (DET/LAM chunks record the runs
+// at their ends for the stitch); grids are persistent and warps stride over
+// units.
 //
 // Memory contract: the series buffer holds at least n + kSeriesPad elements.
 // Blocks are evaluated 32 cells at a time without per-cell bounds on the

@@ -358,11 +358,18 @@ Accrqa_Error enqueue_rr(const T *d_x, int64_t n, int tau, int emb, const T *thr,
 // Stream-ordered scratch of the chunked line walks, from a private memory
 // pool per device that keeps its memory between passes (a pass allocates
 // and frees on its own stream, so passes on different streams never share
-// a buffer).  Null when the pool cannot serve it: the pass then walks its
-// lines whole.
+// a buffer).  Null when the pool cannot serve it, and on a stream that is
+// being captured into a graph (the capture stays free of allocations): the
+// pass then walks its lines whole.
 static void *line_scratch_alloc(size_t bytes, cudaStream_t st) {
     static std::mutex mu;
     static cudaMemPool_t pools[64];
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (cs != cudaStreamCaptureStatusNone) return nullptr;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
         cudaGetLastError();

@@ -263,9 +263,10 @@ Accrqa_Error accrqa_gb300_measures(double *out5, const uint64_t *hist,
  * nthr may exceed 16; passes of 16 are enqueued back to back.  det and lam
  * take the scratch of their chunked walks stream-ordered from a memory pool
  * the library keeps per device (allocated and freed on `stream`, retained
- * between calls); when the pool cannot serve it the lines are walked whole,
- * with the same results.  Callers that may not allocate at all use
- * accrqa_gb300_rr_dev_noalloc (RR only). */
+ * between calls); when the pool cannot serve it, or `stream` is being
+ * captured into a graph, the lines are walked whole, with the same results.
+ * Callers that may not allocate at all use accrqa_gb300_rr_dev_noalloc (RR
+ * only). */
 Accrqa_Error accrqa_gb300_rr_counts_dev(uint64_t *d_counts, const void *d_x,
                                         int32_t dtype, int64_t n, int32_t tau,
                                         int32_t emb, const void *thresholds,

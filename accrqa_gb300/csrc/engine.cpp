@@ -403,6 +403,22 @@ static void *line_scratch_alloc(size_t bytes, cudaStream_t st) {
     return ptr;
 }
 
+// Device bytes the level planes of one pass may take: a third of the free
+// device memory (the passes of several server workers fit side by side).
+static size_t level_budget_bytes() {
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return free_b / 3;
+}
+
+// LAM passes walk their rows from stored tile levels (each unordered pair
+// evaluated once instead of twice) when the planes fit the budget; DET keeps
+// its diagonal walker, which evaluates every pair once already.
+static bool walks_levels(int kind) { return kind == ACCRQA_WALK_LAM; }
+
 template <typename T>
 Accrqa_Error enqueue_lines(int kind, const T *d_x, int64_t n, int tau, int emb,
                            const T *thr, int nthr, int norm, uint64_t *d_hist,
@@ -418,7 +434,14 @@ Accrqa_Error enqueue_lines(int kind, const T *d_x, int64_t n, int tau, int emb,
         const int64_t want = accrqa_gb300_walk_scratch_bytes(&d);
         if (want > 0 && (d.d_scratch = line_scratch_alloc((size_t)want, st)) != nullptr)
             d.scratch_bytes = want;
+        if (d.d_scratch && walks_levels(kind)) {
+            const int64_t pb = accrqa_gb300_walk_plane_bytes(&d);
+            if (pb > 0 && (size_t)pb <= level_budget_bytes() &&
+                (d.d_planes = line_scratch_alloc((size_t)pb, st)) != nullptr)
+                d.planes_bytes = pb;
+        }
         int e = accrqa_gb300_launch_walk(&d, st);
+        if (d.d_planes) cudaFreeAsync(d.d_planes, st);
         if (d.d_scratch) cudaFreeAsync(d.d_scratch, st);
         if (e) return cuda_error((cudaError_t)e, kind == ACCRQA_WALK_DET ? "DET kernel launch" : "LAM kernel launch");
     }

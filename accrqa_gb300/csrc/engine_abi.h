@@ -68,6 +68,13 @@ typedef struct accrqa_walk_desc {
      * same stream.  Without it (or too small) the lines are walked whole. */
     void *d_scratch;
     int64_t scratch_bytes;
+    /* DET/LAM, optional: device memory of accrqa_gb300_walk_plane_bytes()
+     * bytes.  With it (and the chunk-record scratch) the pass first stores
+     * the threshold levels of every upper-triangle tile as bit planes, each
+     * cell evaluated once, and then walks its lines from them -- same
+     * results, a fraction of the distance work. */
+    void *d_planes;
+    int64_t planes_bytes;
 } accrqa_walk_desc;
 
 /* Enqueue one pass on `stream` (a cudaStream_t, 0 = legacy default stream).
@@ -77,6 +84,10 @@ int accrqa_gb300_launch_walk(const accrqa_walk_desc *desc, void *stream);
 /* Scratch bytes the chunked walk of this pass wants (0: none, the lines go
  * whole).  Reads kind, nc and nthr only. */
 int64_t accrqa_gb300_walk_scratch_bytes(const accrqa_walk_desc *desc);
+
+/* Plane bytes of the level walk of this pass (0: the kind has none).  Reads
+ * kind, nc and nthr only. */
+int64_t accrqa_gb300_walk_plane_bytes(const accrqa_walk_desc *desc);
 
 /* Enqueue the recurrence plot of rows [row0, row0 + nrows) into d_out
  * (row-major, nc columns; out_type 1 = int8, 2 = int32). */

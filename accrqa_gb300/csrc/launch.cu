@@ -7,6 +7,7 @@
 
 #include "engine_abi.h"
 #include "rqa_kernels.cuh"
+#include "rqa_planes.cuh"
 
 namespace accrqa {
 
@@ -23,18 +24,30 @@ cudaError_t launch_lam_f64(const accrqa_walk_desc &, cudaStream_t);
 cudaError_t launch_rr_f64f(const accrqa_walk_desc &, cudaStream_t);
 cudaError_t launch_det_f64f(const accrqa_walk_desc &, cudaStream_t);
 cudaError_t launch_lam_f64f(const accrqa_walk_desc &, cudaStream_t);
+cudaError_t launch_levels_f32(const accrqa_walk_desc &, cudaStream_t);
+cudaError_t launch_levels_f64(const accrqa_walk_desc &, cudaStream_t);
+cudaError_t launch_levels_f64f(const accrqa_walk_desc &, cudaStream_t);
 
 int sm_count_cached() {
-    // One value per device ordinal; the engine only ever uses the current one.
+    // One value per device ordinal; the engine only ever uses the current
+    // one.  0 when the device cannot be queried: the launch entry points then
+    // fail with cudaErrorNoDevice instead of sizing a grid for a wrong count.
     static int cache[64];
     static std::mutex mu;
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 1;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+        cudaGetLastError();
+        return 0;
+    }
     std::lock_guard<std::mutex> g(mu);
     if (cache[dev] <= 0) {
         int v = 0;
-        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
-        cache[dev] = v > 0 ? v : 1;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+            v <= 0) {
+            cudaGetLastError();
+            return 0;
+        }
+        cache[dev] = v;
     }
     return cache[dev];
 }
@@ -48,7 +61,7 @@ static cudaError_t launch_rp_t(const void *d_x, int norm, long long nc, int tau,
     const long long blocks = (groups + threads - 1) / threads;
     if (blocks <= 0) return cudaSuccess;
     if (blocks > 0x7FFFFFFFll) return cudaErrorInvalidValue;
-    const T *x = (const T *)d_x + row0 * 0;   // rows are offset inside the kernel
+    const T *x = (const T *)d_x;   // rows are offset inside the kernel
     if (norm == kNormEuclidean)
         rp_cells<T, kNormEuclidean, OUT><<<(unsigned)blocks, threads, 0, st>>>(
             x, nc, tau, emb, key, (OUT *)d_out, row0, nrows);
@@ -119,6 +132,7 @@ extern "C" int accrqa_gb300_launch_compact(const uint64_t *d_hist, int64_t strid
                                            unsigned long long *d_count, void *stream) {
     using namespace accrqa;
     if (nthr <= 0 || p <= 0) return (int)cudaSuccess;
+    if (sm_count_cached() <= 0) return (int)cudaErrorNoDevice;
     const long long warps = (long long)nthr * ((p + 31) / 32);
     long long blocks = (warps + 7) / 8;   // 8 warps of 256 threads
     const long long cap_blocks = (long long)sm_count_cached() * 8;
@@ -150,6 +164,13 @@ extern "C" int64_t accrqa_gb300_walk_scratch_bytes(const accrqa_walk_desc *d) {
     return (int64_t)q.nrecords * nt * 32 * 2 * (int64_t)sizeof(u32);
 }
 
+extern "C" int64_t accrqa_gb300_walk_plane_bytes(const accrqa_walk_desc *d) {
+    using namespace accrqa;
+    if (!d || d->nc < 2 || (d->kind != ACCRQA_WALK_DET && d->kind != ACCRQA_WALK_LAM)) return 0;
+    const int np = d->nthr <= 4 ? Planes<4>::kN : d->nthr <= 8 ? Planes<8>::kN : Planes<16>::kN;
+    return (int64_t)tile_count((d->nc + 31) / 32) * np * 32 * (int64_t)sizeof(u32);
+}
+
 extern "C" int accrqa_gb300_sm_count(void) { return accrqa::sm_count_cached(); }
 
 extern "C" uint64_t accrqa_gb300_launch_count(void) { return accrqa::g_launches.load(); }
@@ -159,6 +180,7 @@ extern "C" int accrqa_gb300_launch_walk(const accrqa_walk_desc *d, void *stream)
     if (!d || d->nthr < 1 || d->nthr > ACCRQA_MAX_THR_PER_PASS || d->nc < 1 ||
         d->tau < 1 || d->emb < 1)
         return (int)cudaErrorInvalidValue;
+    if (sm_count_cached() <= 0) return (int)cudaErrorNoDevice;
     cudaStream_t st = (cudaStream_t)stream;
     cudaError_t e = cudaErrorInvalidValue;
     const bool f64 = d->dtype == ACCRQA_F64;
@@ -168,10 +190,20 @@ extern "C" int accrqa_gb300_launch_walk(const accrqa_walk_desc *d, void *stream)
             e = filt ? launch_rr_f64f(*d, st) : f64 ? launch_rr_f64(*d, st) : launch_rr_f32(*d, st);
             break;
         case ACCRQA_WALK_DET:
-            e = filt ? launch_det_f64f(*d, st) : f64 ? launch_det_f64(*d, st) : launch_det_f32(*d, st);
+            if (d->d_planes)
+                e = filt ? launch_levels_f64f(*d, st) : f64 ? launch_levels_f64(*d, st)
+                                                         : launch_levels_f32(*d, st);
+            else
+                e = filt ? launch_det_f64f(*d, st) : f64 ? launch_det_f64(*d, st)
+                                                        : launch_det_f32(*d, st);
             break;
         case ACCRQA_WALK_LAM:
-            e = filt ? launch_lam_f64f(*d, st) : f64 ? launch_lam_f64(*d, st) : launch_lam_f32(*d, st);
+            if (d->d_planes)
+                e = filt ? launch_levels_f64f(*d, st) : f64 ? launch_levels_f64(*d, st)
+                                                         : launch_levels_f32(*d, st);
+            else
+                e = filt ? launch_lam_f64f(*d, st) : f64 ? launch_lam_f64(*d, st)
+                                                        : launch_lam_f32(*d, st);
             break;
         default: break;
     }
@@ -206,6 +238,7 @@ cudaError_t batch_lam(const accrqa_batch_launch &, cudaStream_t, int *);
 
 static cudaError_t batch_call(const accrqa_batch_launch *L, cudaStream_t st, int *w) {
     if (!L) return cudaErrorInvalidValue;
+    if (sm_count_cached() <= 0) return cudaErrorNoDevice;
     switch (L->kind) {
         case ACCRQA_WALK_RR: return batch_rr(*L, st, w);
         case ACCRQA_WALK_DET: return batch_det(*L, st, w);

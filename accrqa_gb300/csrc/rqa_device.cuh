@@ -76,6 +76,10 @@ struct WalkArgs {
     const float *xhi;
     const float *xlo;
     u64 xkeys[kMaxThrPerPass];
+    // Walks from stored threshold levels (rqa_planes.cuh): the bit planes of
+    // the upper-triangle tiles and the number of 32-row tile bands.
+    u32 *planes;
+    long long tbands;
 };
 
 // ---------------------------------------------------------------------------

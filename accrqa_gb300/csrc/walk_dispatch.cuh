@@ -10,6 +10,7 @@
 
 #include "engine_abi.h"
 #include "rqa_kernels.cuh"
+#include "rqa_planes.cuh"
 
 namespace accrqa {
 
@@ -19,41 +20,21 @@ extern std::atomic<unsigned long long> g_launches;
 // Filter limit pair of a padding slot: (-inf, -inf), surely not recurrent.
 constexpr u64 kNeverFilterPair = 0xFF800000FF800000ull;
 
-template <int KIND, typename T, int NORM, int EMB, int NT>
-static cudaError_t launch_one(const accrqa_walk_desc &d, cudaStream_t st) {
-    void (*kern)(WalkArgs);
-    size_t smem = 0;
-    // if constexpr: a translation unit instantiates only its own kind
-    if constexpr (KIND == ACCRQA_WALK_RR) {
-        kern = rr_rows<T, NORM, EMB, NT>;
-    } else if constexpr (KIND == ACCRQA_WALK_DET) {
-        kern = det_diags<T, NORM, EMB, NT>;
-        smem = LineSmem<NT>::kBytes;
-    } else {
-        kern = lam_rows<T, NORM, EMB, NT>;
-        smem = LineSmem<NT>::kBytes;
-    }
-    // Resident CTAs per SM for this instantiation, computed once (threads
-    // that race on the first call compute the same value).
-    static std::atomic<int> per_sm_cache{-1};
-    int per_sm = per_sm_cache.load();
-    if (per_sm < 0) {
-        int v = 0;
-        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &v, kern, kWarpsPerCta * 32, smem);
-        if (e != cudaSuccess) return e;
-        per_sm = v > 0 ? v : 1;
-        per_sm_cache.store(per_sm);
-    }
-    WalkArgs a;
+// Dispatch tag of the level walks (DET or LAM from stored tile levels, the
+// pass kind read at run time); not a walk kind of the ABI.
+constexpr int kWalkLevels = 3;
+
+// The pass descriptor as kernel arguments: slots in decreasing threshold
+// order (see WalkArgs), the caller's order kept in row[], padding keys the
+// never-recurrent minimum.
+template <typename T>
+static void fill_walk_args(const accrqa_walk_desc &d, WalkArgs &a) {
+    memset(&a, 0, sizeof(a));
     a.x = d.d_x;
     a.nc = d.nc;
     a.tau = d.tau;
     a.emb = d.emb;
     a.nthr = d.nthr;
-    a.pad_ = 0;
-    // Slots in decreasing threshold order (see WalkArgs); the caller's order
-    // is kept in row[].  Padding keys are the never-recurrent minimum.
     int order[kMaxThrPerPass];
     for (int k = 0; k < kMaxThrPerPass; k++) order[k] = k;
     auto wider = [&](int u, int v) {
@@ -92,8 +73,128 @@ static cudaError_t launch_one(const accrqa_walk_desc &d, cudaStream_t st) {
     a.hist = (u64 *)d.d_hist;
     a.hist_stride = d.hist_stride;
     a.maxlen = d.d_maxlen;
-    a.lead = nullptr;
-    a.trail = nullptr;
+}
+
+// Resident CTAs per SM of one kernel instantiation, computed once per
+// instantiation (threads that race on the first call compute the same value).
+template <class K>
+static cudaError_t per_sm_of(K kern, size_t smem, std::atomic<int> &cache, int *out) {
+    int per_sm = cache.load();
+    if (per_sm < 0) {
+        int v = 0;
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &v, kern, kWarpsPerCta * 32, smem);
+        if (e != cudaSuccess) return e;
+        per_sm = v > 0 ? v : 1;
+        cache.store(per_sm);
+    }
+    *out = per_sm;
+    return cudaSuccess;
+}
+
+// (band, chunk) units of equal size over the upper-triangle tiles of
+// `bands` 32-row bands, about 8 per resident warp or more (the RR walk and
+// the level walk's first phase).
+static void plan_upper_units(long long bands, long long resident, long long *chunk,
+                             long long *nunits) {
+    const long long total_blocks = bands * (bands + 1) / 2;
+    long long B = total_blocks / (8 * resident);
+    B = B < 8 ? 8 : (B > 256 ? 256 : B);
+    *chunk = B;
+    *nunits = bands * ((bands + B - 1) / B);
+}
+
+// Join the runs that cross chunk boundaries (same stream, after the walk).
+template <int NT>
+static cudaError_t launch_stitch(const WalkArgs &a, bool det, cudaStream_t st) {
+    const long long lines = a.nbands * NT * 32;
+    long long sgrid = (lines + 255) / 256;
+    const long long scap = (long long)sm_count_cached() * 8;
+    if (sgrid > scap) sgrid = scap;
+    line_stitch<NT><<<(unsigned)sgrid, 256, LineSmem<NT>::kBytes, st>>>(a, det ? 1 : 0);
+    g_launches.fetch_add(1);
+    return cudaGetLastError();
+}
+
+// Persistent grid of `units` warp units: resident CTAs x SMs at most.
+static int grid_for(long long units, int per_sm) {
+    const long long want = (units + kWarpsPerCta - 1) / kWarpsPerCta;
+    const long long cap = (long long)sm_count_cached() * per_sm;
+    return (int)(want < cap ? want : cap);
+}
+
+// The level walk of one DET/LAM pass (rqa_planes.cuh): tile_levels stores
+// the levels of the upper-triangle tiles to d.d_planes, then det_levels or
+// lam_levels walks the lines from them in lam_rows' / det_diags' units, and
+// the stitch joins the chunks -- all on `st`, in that order.
+template <typename T, int NORM, int EMB, int NT>
+static cudaError_t launch_levels_one(const accrqa_walk_desc &d, cudaStream_t st) {
+    constexpr int NP = Planes<NT>::kN;
+    const bool det = d.kind == ACCRQA_WALK_DET;
+    if (!det && d.kind != ACCRQA_WALK_LAM) return cudaErrorInvalidValue;
+    const long long T_ = (d.nc + 31) / 32;
+    const long long need = tile_count(T_) * NP * 32 * (long long)sizeof(u32);
+    if (!d.d_planes || d.planes_bytes < need) return cudaErrorInvalidValue;
+    WalkArgs a;
+    fill_walk_args<T>(d, a);
+    a.planes = (u32 *)d.d_planes;
+    a.tbands = T_;
+
+    static std::atomic<int> c_tiles{-1}, c_det{-1}, c_lam{-1};
+    int per1 = 0, per2 = 0;
+    cudaError_t e = per_sm_of(tile_levels<T, NORM, EMB, NT>, 0, c_tiles, &per1);
+    if (e != cudaSuccess) return e;
+    void (*walk)(WalkArgs) = det ? det_levels<NT> : lam_levels<NT>;
+    e = per_sm_of(walk, LineSmem<NT>::kBytes, det ? c_det : c_lam, &per2);
+    if (e != cudaSuccess) return e;
+
+    plan_upper_units(T_, (long long)sm_count_cached() * per1 * kWarpsPerCta, &a.chunk,
+                     &a.nunits);
+    tile_levels<T, NORM, EMB, NT><<<grid_for(a.nunits, per1), kWarpsPerCta * 32, 0, st>>>(a);
+    g_launches.fetch_add(1);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+
+    // chunked when the caller's scratch holds the boundary records
+    LinePlan q = plan_lines(det, d.nc, sm_count_cached(), d.d_scratch != nullptr);
+    const long long rec = q.nrecords * NT * 32 * 2 * (long long)sizeof(u32);
+    if (q.nrecords > 0 && rec > d.scratch_bytes)
+        q = plan_lines(det, d.nc, sm_count_cached(), false);
+    a.nbands = q.nbands;
+    a.nunits = q.nunits;
+    a.chunk = q.chunk;
+    a.lead = a.trail = nullptr;
+    if (q.nrecords > 0) {
+        a.lead = (u32 *)d.d_scratch;
+        a.trail = a.lead + q.nrecords * NT * 32;
+    }
+    if (a.nunits <= 0) return cudaSuccess;
+    walk<<<grid_for(a.nunits, per2), kWarpsPerCta * 32, LineSmem<NT>::kBytes, st>>>(a);
+    g_launches.fetch_add(1);
+    if ((e = cudaGetLastError()) != cudaSuccess || q.nrecords == 0) return e;
+    return launch_stitch<NT>(a, det, st);
+}
+
+template <int KIND, typename T, int NORM, int EMB, int NT>
+static cudaError_t launch_one(const accrqa_walk_desc &d, cudaStream_t st) {
+    if constexpr (KIND == kWalkLevels) return launch_levels_one<T, NORM, EMB, NT>(d, st);
+    void (*kern)(WalkArgs);
+    size_t smem = 0;
+    // if constexpr: a translation unit instantiates only its own kind
+    if constexpr (KIND == ACCRQA_WALK_RR) {
+        kern = rr_rows<T, NORM, EMB, NT>;
+    } else if constexpr (KIND == ACCRQA_WALK_DET) {
+        kern = det_diags<T, NORM, EMB, NT>;
+        smem = LineSmem<NT>::kBytes;
+    } else {
+        kern = lam_rows<T, NORM, EMB, NT>;
+        smem = LineSmem<NT>::kBytes;
+    }
+    static std::atomic<int> per_sm_cache{-1};
+    int per_sm = 0;
+    cudaError_t e0 = per_sm_of(kern, smem, per_sm_cache, &per_sm);
+    if (e0 != cudaSuccess) return e0;
+    WalkArgs a;
+    fill_walk_args<T>(d, a);
     LinePlan q{};
     if (KIND != ACCRQA_WALK_RR) {
         // chunked when the caller's scratch holds the boundary records
@@ -110,33 +211,16 @@ static cudaError_t launch_one(const accrqa_walk_desc &d, cudaStream_t st) {
             a.trail = a.lead + q.nrecords * NT * 32;
         }
     } else {
-        // (band, chunk) units of equal size, about 8 per resident warp or more
         a.nbands = (d.nc + 31) / 32;
-        const long long nblk0 = a.nbands;                        // blocks of band 0's walk
-        const long long total_blocks = a.nbands * (nblk0 + 1) / 2;
-        const long long resident = (long long)sm_count_cached() * per_sm * kWarpsPerCta;
-        long long B = total_blocks / (8 * resident);
-        B = B < 8 ? 8 : (B > 256 ? 256 : B);
-        a.chunk = B;
-        a.nunits = a.nbands * ((nblk0 + B - 1) / B);
+        plan_upper_units(a.nbands, (long long)sm_count_cached() * per_sm * kWarpsPerCta,
+                         &a.chunk, &a.nunits);
     }
     if (a.nunits <= 0) return cudaSuccess;
-    long long want = (a.nunits + kWarpsPerCta - 1) / kWarpsPerCta;
-    long long cap = (long long)sm_count_cached() * per_sm;
-    int grid = (int)(want < cap ? want : cap);
-    kern<<<grid, kWarpsPerCta * 32, smem, st>>>(a);
+    kern<<<grid_for(a.nunits, per_sm), kWarpsPerCta * 32, smem, st>>>(a);
     g_launches.fetch_add(1);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || q.nrecords == 0) return e;
-    // join the runs that cross chunk boundaries (same stream, after the walk)
-    const long long lines = q.nbands * NT * 32;
-    long long sgrid = (lines + 255) / 256;
-    const long long scap = (long long)sm_count_cached() * 8;
-    if (sgrid > scap) sgrid = scap;
-    line_stitch<NT><<<(unsigned)sgrid, 256, LineSmem<NT>::kBytes, st>>>(
-        a, KIND == ACCRQA_WALK_DET ? 1 : 0);
-    g_launches.fetch_add(1);
-    return cudaGetLastError();
+    return launch_stitch<NT>(a, KIND == ACCRQA_WALK_DET, st);
 }
 
 template <int KIND, typename T, int NORM, int EMB>

@@ -1,0 +1,3 @@
+// Kernel instantiations for the DET/LAM level walks on double series.
+#include "walk_dispatch.cuh"
+ACCRQA_DEFINE_WALK_TU(launch_levels_f64, kWalkLevels, double)

@@ -1,12 +1,17 @@
-"""GPU: chunked line walks equal whole-line walks, bit for bit.
+"""GPU: chunked line walks equal whole-line walks, and level walks equal
+distance walks, bit for bit.
 
 The DET/LAM kernels split lines into equal chunks when the caller gives
 scratch for the chunk boundary records, and join the runs that cross chunk
-boundaries in a second kernel.  Here the same pass is enqueued through the
-kernel library's C ABI (accrqa_gb300_launch_walk) with and without scratch,
-and the histograms and longest-line markers must be identical -- with a
-threshold that makes every cell recurrent (every chunk full, one run per
-line), one that makes almost none recurrent, and a spread between.
+boundaries in a second kernel.  Given plane memory as well, they first store
+the threshold levels of every upper-triangle tile and walk the lines from
+those (each unordered pair evaluated once).  Here the same pass is enqueued
+through the kernel library's C ABI (accrqa_gb300_launch_walk) with and
+without scratch and planes, and the histograms and longest-line markers must
+be identical -- with a threshold that makes every cell recurrent (every
+chunk full, one run per line), one that makes almost none recurrent, and a
+spread between; with 4, 8 and 16 slots, series lengths that are and are not
+multiples of the 32-cell tiles, and both norms.
 """
 import ctypes
 
@@ -33,10 +38,11 @@ class WalkDesc(ctypes.Structure):
         ("d_xhi", ctypes.c_void_p), ("d_xlo", ctypes.c_void_p),
         ("filter_keys", ctypes.c_uint64 * MAX_THR),
         ("d_scratch", ctypes.c_void_p), ("scratch_bytes", ctypes.c_int64),
+        ("d_planes", ctypes.c_void_p), ("planes_bytes", ctypes.c_int64),
     ]
 
 
-def _walk(torch, lib, kind, dx, dt, n, tau, emb, thr, norm, chunked):
+def _walk(torch, lib, kind, dx, dt, n, tau, emb, thr, norm, chunked, levels=False):
     nc = n - (emb - 1) * tau
     keys = engine.threshold_keys(thr, dt, norm)
     hist = torch.zeros((len(thr), nc + 1), dtype=torch.int64, device="cuda")
@@ -54,10 +60,23 @@ def _walk(torch, lib, kind, dx, dt, n, tau, emb, thr, norm, chunked):
         assert want > 0, "this size must chunk"
         scratch = torch.empty(want, dtype=torch.uint8, device="cuda")
         d.d_scratch, d.scratch_bytes = scratch.data_ptr(), want
+    planes = None
+    if levels:
+        pb = lib.accrqa_gb300_walk_plane_bytes(ctypes.byref(d))
+        assert pb > 0
+        planes = torch.empty(pb, dtype=torch.uint8, device="cuda")
+        d.d_planes, d.planes_bytes = planes.data_ptr(), pb
     st = torch.cuda.current_stream().cuda_stream
     assert lib.accrqa_gb300_launch_walk(ctypes.byref(d), ctypes.c_void_p(st)) == 0
     torch.cuda.synchronize()
     return hist.cpu().numpy(), mx.cpu().numpy()[:len(thr)]
+
+
+def _bind(lib):
+    for f in (lib.accrqa_gb300_walk_scratch_bytes, lib.accrqa_gb300_walk_plane_bytes):
+        f.restype = ctypes.c_int64
+        f.argtypes = [ctypes.c_void_p]
+    lib.accrqa_gb300_launch_walk.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
 
 
 @pytest.mark.parametrize("dt", [np.float32, np.float64])
@@ -66,9 +85,7 @@ def _walk(torch, lib, kind, dx, dt, n, tau, emb, thr, norm, chunked):
 def test_chunked_equals_whole(kind, dt, n, tau, emb, norm):
     torch = pytest.importorskip("torch")
     lib = _lib.handle()
-    lib.accrqa_gb300_walk_scratch_bytes.restype = ctypes.c_int64
-    lib.accrqa_gb300_walk_scratch_bytes.argtypes = [ctypes.c_void_p]
-    lib.accrqa_gb300_launch_walk.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    _bind(lib)
     x = workloads.logistic(n, 7 + n).astype(dt)
     # 0: exact matches only; 4.0: beyond the largest distance (all recurrent)
     thr = np.array([0.0, 0.01, 0.05, 0.1, 0.2, 0.3, 0.5, 0.8, 1.2, 4.0], dtype=dt)
@@ -84,3 +101,26 @@ def test_chunked_equals_whole(kind, dt, n, tau, emb, norm):
         assert h0[-1, nc] == nc          # every row one run of nc cells
     else:
         assert h0[-1, 1:].sum() == nc - 1  # every strict-upper diagonal one run
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+@pytest.mark.parametrize("kind", [WALK_DET, WALK_LAM])
+@pytest.mark.parametrize("nthr", [3, 8, 10])
+@pytest.mark.parametrize("n,tau,emb,norm", [(20000, 1, 3, 1), (9000, 2, 5, 2), (3001, 1, 1, 1),
+                                            (4096, 3, 4, 2), (97, 1, 2, 1), (33, 1, 1, 2)])
+def test_levels_equal_distance_walk(kind, dt, nthr, n, tau, emb, norm):
+    torch = pytest.importorskip("torch")
+    lib = _lib.handle()
+    _bind(lib)
+    x = workloads.logistic(n, 11 + n).astype(dt)
+    thr = np.array([0.0, 0.01, 0.05, 0.1, 0.2, 0.3, 0.5, 0.8, 1.2, 4.0], dtype=dt)
+    thr = thr[np.linspace(0, len(thr) - 1, nthr).astype(int)] if nthr <= len(thr) else thr
+    dx = torch.zeros(n + 128, dtype=torch.float32 if dt == np.float32 else torch.float64,
+                     device="cuda")
+    dx[:n] = torch.from_numpy(x).cuda()
+    h0, m0 = _walk(torch, lib, kind, dx, dt, n, tau, emb, thr, norm, chunked=False)
+    chunked = n >= 3000   # these sizes split their lines into chunks
+    for ch in ([False, True] if chunked else [False]):
+        h1, m1 = _walk(torch, lib, kind, dx, dt, n, tau, emb, thr, norm, chunked=ch, levels=True)
+        np.testing.assert_array_equal(h1, h0)
+        np.testing.assert_array_equal(m1, m0)

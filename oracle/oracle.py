@@ -26,12 +26,13 @@ _i64 = ctypes.c_int64
 
 
 def build(quiet: bool = True) -> None:
-    """Compile liboracle.so (and the reference build when its sources exist)."""
+    """Compile liboracle.so, and the reference's own CPU code into _ref/ when
+    ACCRQA_REFERENCE_TREE names a reference source tree (skipped otherwise)."""
     out = subprocess.DEVNULL if quiet else None
     subprocess.run(["make", "-s", "-C", _HERE, "liboracle.so"], check=True,
                    stdout=out)
-    ref_root = os.environ.get("ACCRQA_REFERENCE_TREE", "/root/reference")
-    if os.path.isdir(os.path.join(ref_root, "src")):
+    ref_root = os.environ.get("ACCRQA_REFERENCE_TREE", "")
+    if ref_root and os.path.isdir(os.path.join(ref_root, "src")):
         subprocess.run(["make", "-s", "-C", _HERE, "ref", f"REF={ref_root}"],
                        check=True, stdout=out)
 

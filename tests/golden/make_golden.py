@@ -1,10 +1,10 @@
 """Generate the golden fixtures in tests/golden/ from the AccRQA reference tree.
 
-Run in a container that has the reference sources (default /root/reference,
-override with ACCRQA_REFERENCE_TREE) after `make -C oracle ref`, which builds
-the reference's own CPU code into oracle/_ref/libaccrqa_ref.so:
+Run where the reference sources are, named by ACCRQA_REFERENCE_TREE, after
+`make -C oracle ref REF=<tree>`, which builds the reference's own CPU code
+into oracle/_ref/libaccrqa_ref.so:
 
-    python tests/golden/make_golden.py
+    ACCRQA_REFERENCE_TREE=<tree> python tests/golden/make_golden.py
 
 Outputs (all small, committed):
   crqa_input.npy          the 1122-sample series of the reference's CRQA
@@ -32,7 +32,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
-REF = os.environ.get("ACCRQA_REFERENCE_TREE", "/root/reference")
+REF = os.environ.get("ACCRQA_REFERENCE_TREE", "")
 
 
 # ---------------------------------------------------------------------------
@@ -175,6 +175,8 @@ def crqa_kat():
 
 
 def main():
+    if not REF or not os.path.isdir(os.path.join(REF, "src")):
+        raise SystemExit("set ACCRQA_REFERENCE_TREE to the AccRQA reference source tree")
     from oracle import oracle
     oracle.build()
     if oracle.ref_lib() is None:

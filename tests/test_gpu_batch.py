@@ -64,6 +64,37 @@ def test_batch_counts_match_oracle(gpu, oracle_mod):
         assert "det" not in o
 
 
+RTOL = {np.float32: 1e-6, np.float64: 1e-12}
+
+
+@pytest.mark.parametrize("measures", [("det", "lam"), ("rr", "det", "lam"), ("lam",)])
+def test_batch_lines_match_oracle(gpu, oracle_mod, measures):
+    """Batched DET and LAM outputs against the oracle's histograms (their
+    measures in the reference's GPU layout and conventions): ratios within
+    1e-6 (float32) / 1e-12 (float64), line lengths exact."""
+    jobs = _jobs(11, 14)
+    outs = engine.batch(jobs, measures=measures)
+    for j, o in zip(jobs, outs):
+        x, dt = j["x"], j["x"].dtype.type
+        for kind in ("det", "lam"):
+            if kind not in measures:
+                assert kind not in o
+                continue
+            lm = j["lmin"] if kind == "det" else j["vmin"]
+            want = oracle_mod.line_output(x, [j["tau"]], [j["emb"]], [lm], j["thresholds"],
+                                          j["norm"], j["calc_entr"], kind == "det").reshape(-1, 5)
+            got = np.asarray(o[kind], np.float64)
+            w = np.asarray(want, np.float64)
+            assert np.array_equal(np.isnan(got), np.isnan(w)), kind
+            m = ~np.isnan(w)
+            np.testing.assert_allclose(got[m], w[m], rtol=RTOL[dt], atol=0)
+            np.testing.assert_array_equal(got[:, 2], w[:, 2])   # longest line
+        if "rr" in measures:
+            nc = len(x) - (j["emb"] - 1) * j["tau"]
+            cnt = oracle_mod.rr_counts(x, j["tau"], j["emb"], j["thresholds"], j["norm"])
+            np.testing.assert_array_equal(o["rr"], oracle_mod.rr_output(cnt, nc, x.dtype))
+
+
 def test_batch_rejects_bad_job(gpu):
     jobs = _jobs(3, 2)
     jobs[1]["tau"] = 0

@@ -149,3 +149,21 @@ def test_constant_series_answers(oracle_mod, tau):
             m = oracle_mod.measures(hl, vm, False)
             assert m[0] == 1.0 and m[4] == 1.0
         assert oracle_mod.rr_counts(x, tau, 1, [thr], 2)[0] == 100
+
+
+def test_fullsize_series_regenerate():
+    """The full-size GPU parity fixtures (tests/golden/fullsize.*) were
+    recorded on seeded series: regenerated here they hash the same, so the GPU
+    tests compare the engine with the reference on the very same input."""
+    import json
+    import sys
+    gold = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    sys.path.insert(0, gold)
+    import make_fullsize
+    with open(os.path.join(gold, "fullsize.json")) as f:
+        table = {c["name"]: c for c in json.load(f)["cases"]}
+    for name, build, combos, thr_of, _ in make_fullsize.cases():
+        x = build()
+        assert make_fullsize.series_sha(x) == table[name]["sha256"], name
+        thr = thr_of(x)
+        assert [t.tobytes().hex() for t in thr] == table[name]["thresholds_hex"], name

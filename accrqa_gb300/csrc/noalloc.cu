@@ -32,7 +32,10 @@ namespace {
 
 // Device address of the scratch array, looked up once per device.  In host
 // code the name g_rr_noalloc_counts is only a host-side stand-in for the
-// symbol, not a device address, so kernels must be given this pointer.
+// symbol, not a device address, so kernels must be given this pointer.  The
+// cached address belongs to the device's primary context: it is not valid
+// after cudaDeviceReset (which ends that context); a process that resets a
+// device must not call this entry point on it again.
 std::mutex g_mu;
 void *g_scratch[64];
 
@@ -77,6 +80,11 @@ extern "C" Accrqa_Error accrqa_gb300_rr_dev_noalloc(void *d_rr, const void *d_x,
     if (n < 1 || tau < 1 || emb < 1 || n - (int64_t)(emb - 1) * tau < 1) return ERR_INVALID_ARGUMENT;
     if (norm != DST_EUCLIDEAN && norm != DST_MAXIMAL) return ERR_INVALID_ARGUMENT;
 
+    // keys first: a call that fails validation enqueues nothing
+    uint64_t keys[ACCRQA_NOALLOC_MAX_THR];
+    Accrqa_Error ke = accrqa_gb300_threshold_keys(keys, thresholds, dtype, nthr, norm);
+    if (ke != SUCCESS) return ke;
+
     void *scratch = nullptr;
     cudaError_t e = scratch_for_current_device(&scratch);
     if (e != cudaSuccess) return fail(e);
@@ -86,10 +94,6 @@ extern "C" Accrqa_Error accrqa_gb300_rr_dev_noalloc(void *d_rr, const void *d_x,
     // The array keeps the last call's counts: clear what this call uses.
     e = cudaMemsetAsync(counts, 0, (size_t)nthr * sizeof(unsigned long long), st);
     if (e != cudaSuccess) return fail(e);
-
-    uint64_t keys[ACCRQA_NOALLOC_MAX_THR];
-    Accrqa_Error ke = accrqa_gb300_threshold_keys(keys, thresholds, dtype, nthr, norm);
-    if (ke != SUCCESS) return ke;
     const uint64_t never = dtype == ACCRQA_GB300_F32 ? 0xBF800000ull : 0ull;
     const int64_t nc = n - (int64_t)(emb - 1) * tau;
     for (int k0 = 0; k0 < nthr; k0 += ACCRQA_MAX_THR_PER_PASS) {

@@ -208,6 +208,8 @@ void accrqa_gb300_transfer_stats(uint64_t *h2d_bytes, uint64_t *d2h_bytes, int32
 
 uint64_t accrqa_gb300_kernel_launches(void) { return accrqa_gb300_launch_count(); }
 
+void accrqa_gb300_test_fail_allocations(int32_t count) { set_alloc_faults(count); }
+
 Accrqa_Error accrqa_gb300_batch(const accrqa_gb300_series_job *jobs, int32_t njobs) {
     return run_batch(jobs, njobs);
 }

@@ -31,7 +31,7 @@ void set_last_error(const char *fmt, ...) {
 const char *last_error() { return g_last_error; }
 
 // Host-side phase trace on stderr, enabled by ACCRQA_GB300_TRACE=1.
-static bool trace_on() {
+bool trace_on() {
     static const bool on = [] {
         const char *v = std::getenv("ACCRQA_GB300_TRACE");
         return v && v[0] == '1';
@@ -39,7 +39,7 @@ static bool trace_on() {
     return on;
 }
 
-static void trace(const char *fmt, ...) {
+void trace(const char *fmt, ...) {
     if (!trace_on()) return;
     static const auto t0 = std::chrono::steady_clock::now();
     const double ms = std::chrono::duration<double, std::milli>(
@@ -103,16 +103,41 @@ void transfer_stats(uint64_t *h2d, uint64_t *d2h, int reset) {
 // ===========================================================================
 // Device memory and contexts
 // ===========================================================================
+// Injected allocation failures (accrqa_gb300_test_fail_allocations): the
+// next N device allocations of the engine fail with
+// cudaErrorMemoryAllocation before reaching the driver.  A host-side fake of
+// the failing call, so that the error paths can be tested without exhausting
+// device memory.
+static std::atomic<int> g_fail_allocs{0};
+
+void set_alloc_faults(int count) { g_fail_allocs.store(count > 0 ? count : 0); }
+
+bool alloc_fault() {
+    int v = g_fail_allocs.load();
+    while (v > 0) {
+        if (g_fail_allocs.compare_exchange_weak(v, v - 1)) return true;
+    }
+    return false;
+}
+
+static cudaError_t device_malloc(void **p, size_t bytes) {
+    if (alloc_fault()) {
+        *p = nullptr;
+        return cudaErrorMemoryAllocation;
+    }
+    return cudaMalloc(p, bytes);
+}
+
 cudaError_t DeviceBuffer::reserve(size_t need) {
     if (need <= bytes && ptr) return cudaSuccess;
     release();
     size_t grow = need + need / 4 + 4096;
-    cudaError_t e = cudaMalloc(&ptr, grow);
+    cudaError_t e = device_malloc(&ptr, grow);
     if (e != cudaSuccess) {
         ptr = nullptr;
         bytes = 0;
         cudaGetLastError();
-        e = cudaMalloc(&ptr, need);   // retry without headroom
+        e = device_malloc(&ptr, need);   // retry without headroom
         if (e != cudaSuccess) {
             ptr = nullptr;
             return e;
@@ -741,16 +766,20 @@ static Accrqa_Error fetch_histograms(Context &c, int kind, const uint64_t *d_his
 // ===========================================================================
 // API-level drivers
 // ===========================================================================
+// `pre`: the series is already on the device (a server's resident request);
+// otherwise it is uploaded from x.
 template <typename T>
 Accrqa_Error run_rr_in(Context *c, T *out, const T *x, size_t n, const int *taus, int ntau,
-                       const int *embs, int nemb, const T *thr, int nthr, int norm) {
+                       const int *embs, int nemb, const T *thr, int nthr, int norm,
+                       const DevSeries<T> *pre = nullptr) {
     Accrqa_Error err = check_norm(norm);
     if (err) return err;
     for (int a = 0; a < ntau; a++)
         for (int b = 0; b < nemb; b++)
             if ((err = check_combo(n, taus[a], embs[b]))) return err;
     DevSeries<T> ds;
-    if ((err = upload_series<T>(*c, x, (int64_t)n, &ds))) return err;
+    if (pre) ds = *pre;
+    else if ((err = upload_series<T>(*c, x, (int64_t)n, &ds))) return err;
     const T *d_x = ds.x;
     const size_t ncnt = (size_t)ntau * nemb * nthr;
     CU(c->counts.reserve(ncnt * 8), "cudaMalloc(counts)");
@@ -784,7 +813,8 @@ Accrqa_Error run_rr_in(Context *c, T *out, const T *x, size_t n, const int *taus
 template <typename T>
 Accrqa_Error run_lines_in(Context *c, int kind, T *out, const T *x, size_t n, const int *taus,
                           int ntau, const int *embs, int nemb, const int *lmins,
-                          int nl, const T *thr, int nthr, int norm, int calc_entr) {
+                          int nl, const T *thr, int nthr, int norm, int calc_entr,
+                          const DevSeries<T> *pre = nullptr) {
     Accrqa_Error err = check_norm(norm);
     if (err) return err;
     int lmin_max = 0;
@@ -803,7 +833,8 @@ Accrqa_Error run_lines_in(Context *c, int kind, T *out, const T *x, size_t n, co
     const bool is_det = kind == ACCRQA_WALK_DET;
 
     DevSeries<T> ds;
-    if ((err = upload_series<T>(*c, x, (int64_t)n, &ds))) return err;
+    if (pre) ds = *pre;
+    else if ((err = upload_series<T>(*c, x, (int64_t)n, &ds))) return err;
     const T *d_x = ds.x;
 
     const size_t budget = line_budget_bytes();
@@ -896,6 +927,51 @@ Accrqa_Error run_lines(int kind, T *out, const T *x, size_t n, const int *taus,
     std::lock_guard<std::mutex> g(c->mu);
     return run_lines_in<T>(c, kind, out, x, n, taus, ntau, embs, nemb, lmins, nl, thr, nthr,
                            norm, calc_entr);
+}
+
+// One series job on a device-resident series (the job's x is not read):
+// the passes go on c.stream, which the caller has ordered after the upload.
+Accrqa_Error run_job_resident(Context &c, const accrqa_gb300_series_job &J,
+                              const ResidentSeries &rs) {
+    Accrqa_Error err = SUCCESS;
+    const int tau = J.tau, emb = J.emb, lmin = J.lmin, vmin = J.vmin;
+    if (J.dtype == ACCRQA_GB300_F32) {
+        DevSeries<float> ds;
+        ds.x = (const float *)rs.x;
+        const float *thr = (const float *)J.thresholds;
+        if (J.rr_out && (err = run_rr_in<float>(&c, (float *)J.rr_out, nullptr, (size_t)J.n, &tau,
+                                                1, &emb, 1, thr, J.nthr, J.norm, &ds)))
+            return err;
+        if (J.det_out && (err = run_lines_in<float>(&c, ACCRQA_WALK_DET, (float *)J.det_out,
+                                                    nullptr, (size_t)J.n, &tau, 1, &emb, 1, &lmin,
+                                                    1, thr, J.nthr, J.norm, J.calc_entr, &ds)))
+            return err;
+        if (J.lam_out && (err = run_lines_in<float>(&c, ACCRQA_WALK_LAM, (float *)J.lam_out,
+                                                    nullptr, (size_t)J.n, &tau, 1, &emb, 1, &vmin,
+                                                    1, thr, J.nthr, J.norm, J.calc_entr, &ds)))
+            return err;
+    } else {
+        DevSeries<double> ds;
+        ds.x = (const double *)rs.x;
+        ds.hi = rs.hi;
+        ds.lo = rs.lo;
+        ds.maxabs = rs.maxabs;
+        const double *thr = (const double *)J.thresholds;
+        if (J.rr_out && (err = run_rr_in<double>(&c, (double *)J.rr_out, nullptr, (size_t)J.n,
+                                                 &tau, 1, &emb, 1, thr, J.nthr, J.norm, &ds)))
+            return err;
+        if (J.det_out && (err = run_lines_in<double>(&c, ACCRQA_WALK_DET, (double *)J.det_out,
+                                                     nullptr, (size_t)J.n, &tau, 1, &emb, 1,
+                                                     &lmin, 1, thr, J.nthr, J.norm, J.calc_entr,
+                                                     &ds)))
+            return err;
+        if (J.lam_out && (err = run_lines_in<double>(&c, ACCRQA_WALK_LAM, (double *)J.lam_out,
+                                                     nullptr, (size_t)J.n, &tau, 1, &emb, 1,
+                                                     &vmin, 1, thr, J.nthr, J.norm, J.calc_entr,
+                                                     &ds)))
+            return err;
+    }
+    return SUCCESS;
 }
 
 // One series job through the per-series path (reference output conventions).

@@ -19,8 +19,11 @@ namespace accrqa {
 
 typedef unsigned long long u64;
 
-// ---- errors ---------------------------------------------------------------
+// ---- errors and tracing -----------------------------------------------------
 void set_last_error(const char *fmt, ...);
+// Host-side phase trace on stderr when ACCRQA_GB300_TRACE=1.
+bool trace_on();
+void trace(const char *fmt, ...);
 const char *last_error();
 Accrqa_Error cuda_error(cudaError_t e, const char *what);
 // Bytes copied host->device and device->host by the engine since load (or
@@ -29,6 +32,11 @@ void transfer_stats(uint64_t *h2d, uint64_t *d2h, int reset);
 void transfer_stats_add(size_t h2d, size_t d2h);
 
 // ---- device memory --------------------------------------------------------
+// Injected allocation failures for tests of the error paths: the next
+// `count` device allocations of the engine fail with
+// cudaErrorMemoryAllocation (alloc_fault() consumes one).
+void set_alloc_faults(int count);
+bool alloc_fault();
 // Grow-only device allocation owned by a context.
 struct DeviceBuffer {
     void *ptr = nullptr;
@@ -158,11 +166,26 @@ Accrqa_Error run_rp_bits(uint32_t *out, const T *x, size_t n, int tau, int emb, 
 // One series job through the per-series path, on a given context.
 Accrqa_Error run_job_plain(Context &c, const accrqa_gb300_series_job &job);
 
+// A series kept on the device (a server's admitted request): the series,
+// padded by ACCRQA_SERIES_PAD elements, and for float64 series that take the
+// float filter its split into hi/lo floats (null otherwise) and max|x|.
+struct ResidentSeries {
+    const void *x = nullptr;
+    const float *hi = nullptr, *lo = nullptr;
+    double maxabs = 0.0;
+};
+// One series job on a resident series; c.stream must be ordered after the
+// series' upload.  Same results as run_job_plain.
+Accrqa_Error run_job_resident(Context &c, const accrqa_gb300_series_job &job,
+                              const ResidentSeries &rs);
+
 // Many series in one submission (accrqa_gb300_batch).
 Accrqa_Error run_batch(const accrqa_gb300_series_job *jobs, int njobs);
 // The same on a given context, in sub-batches of at most `budget` device bytes.
+// With `rs`, a job whose rs[j].x is set reads that resident series instead of
+// uploading its x (c.stream must be ordered after those uploads).
 Accrqa_Error run_batch_in(Context &c, const accrqa_gb300_series_job *jobs, int njobs,
-                          size_t budget);
+                          size_t budget, const ResidentSeries *rs = nullptr);
 // Device bytes one job of a batch needs (series, histograms, work units).
 size_t batch_job_bytes(const accrqa_gb300_series_job &job);
 Accrqa_Error check_batch_job(const accrqa_gb300_series_job &job);

@@ -114,16 +114,22 @@ void write_line_out(void *out, int k, const LineHistogram &h, int lmin, bool ful
 
 }  // namespace
 
-// One sub-batch whose device memory fits; jobs [j0, j1).
+// One sub-batch whose device memory fits; jobs [j0, j1).  Jobs with a
+// resident series (rs[j].x) read it in place; the others are uploaded.
 static Accrqa_Error run_batch_part(Context &c, const accrqa_gb300_series_job *jobs, int j0,
-                                   int j1) {
+                                   int j1, const ResidentSeries *rs) {
     // ---- plan -------------------------------------------------------------
     std::vector<size_t> xoff((size_t)(j1 - j0)), hioff((size_t)(j1 - j0), 0);
     std::vector<double> maxabs((size_t)(j1 - j0), -1.0);   // >= 0: float64 job takes the filter
     size_t series_bytes = 0;
+    auto resident = [&](int j) { return rs && rs[j].x; };
     for (int j = j0; j < j1; j++) {
         const size_t es = jobs[j].dtype == ACCRQA_GB300_F32 ? 4 : 8;
         const size_t jj = (size_t)(j - j0);
+        if (resident(j)) {
+            if (rs[j].hi && rs[j].lo) maxabs[jj] = rs[j].maxabs;
+            continue;
+        }
         xoff[jj] = series_bytes;
         series_bytes = align16(series_bytes + (size_t)(jobs[j].n + ACCRQA_SERIES_PAD) * es);
         double m = 0.0;
@@ -283,6 +289,8 @@ static Accrqa_Error run_batch_part(Context &c, const accrqa_gb300_series_job *jo
     }
     const size_t arena_bytes = align16(off);
 
+    trace("batch [%d, %d): %zu passes, %zu groups planned, arena %zu MB", j0, j1,
+          passes.size(), plans.size(), arena_bytes >> 20);
     // ---- stage ------------------------------------------------------------
     CUB(c.arena.reserve(arena_bytes), "cudaMalloc(batch arena)");
     char *dev = (char *)c.arena.ptr;
@@ -290,6 +298,7 @@ static Accrqa_Error run_batch_part(Context &c, const accrqa_gb300_series_job *jo
     CUB(pinned_reserve(c, upload_end), "cudaHostAlloc(batch staging)");
     char *host = (char *)c.pinned;
     for (int j = j0; j < j1; j++) {
+        if (resident(j)) continue;
         const size_t es = jobs[j].dtype == ACCRQA_GB300_F32 ? 4 : 8;
         char *dst = host + xoff[(size_t)(j - j0)];
         std::memcpy(dst, jobs[j].x, (size_t)jobs[j].n * es);
@@ -308,11 +317,19 @@ static Accrqa_Error run_batch_part(Context &c, const accrqa_gb300_series_job *jo
         for (accrqa_batch_job &d : gp.table) {
             const Pass &p = passes[(size_t)d.pad_];
             d.pad_ = 0;
-            d.x = dev + xoff[(size_t)(p.job - j0)];
-            if (maxabs[(size_t)(p.job - j0)] >= 0.0) {
-                const size_t ho = hioff[(size_t)(p.job - j0)];
-                d.xhi = (const float *)(dev + ho);
-                d.xlo = (const float *)(dev + ho) + (jobs[p.job].n + ACCRQA_SERIES_PAD);
+            if (resident(p.job)) {
+                d.x = rs[p.job].x;
+                if (maxabs[(size_t)(p.job - j0)] >= 0.0) {
+                    d.xhi = rs[p.job].hi;
+                    d.xlo = rs[p.job].lo;
+                }
+            } else {
+                d.x = dev + xoff[(size_t)(p.job - j0)];
+                if (maxabs[(size_t)(p.job - j0)] >= 0.0) {
+                    const size_t ho = hioff[(size_t)(p.job - j0)];
+                    d.xhi = (const float *)(dev + ho);
+                    d.xlo = (const float *)(dev + ho) + (jobs[p.job].n + ACCRQA_SERIES_PAD);
+                }
             }
             d.counts = p.kind == ACCRQA_WALK_RR ? (uint64_t *)(dev + p.counts_off) : nullptr;
             d.maxlen = p.kind != ACCRQA_WALK_RR ? (uint32_t *)(dev + p.maxlen_off) : nullptr;
@@ -326,8 +343,9 @@ static Accrqa_Error run_batch_part(Context &c, const accrqa_gb300_series_job *jo
         gp.L.d_warp_begin = (const int32_t *)(dev + gp.ranges_off);
     }
     // series and tables in two copies (the result region between them is zeroed)
-    CUB(cudaMemcpyAsync(dev, host, series_bytes, cudaMemcpyHostToDevice, c.stream),
-        "cudaMemcpy(batch series)");
+    if (series_bytes)
+        CUB(cudaMemcpyAsync(dev, host, series_bytes, cudaMemcpyHostToDevice, c.stream),
+            "cudaMemcpy(batch series)");
     if (arena_bytes > zero_end)
         CUB(cudaMemcpyAsync(dev + zero_end, host + zero_end, arena_bytes - zero_end,
                             cudaMemcpyHostToDevice, c.stream), "cudaMemcpy(batch tables)");
@@ -381,6 +399,7 @@ static Accrqa_Error run_batch_part(Context &c, const accrqa_gb300_series_job *jo
         transfer_stats_add(0, head_end - zero_begin);
     }
     CUB(cudaStreamSynchronize(c.stream), "batched kernels");
+    trace("batch: kernels done");
     // histogram prefixes
     std::vector<std::vector<uint64_t>> pref(passes.size());
     std::vector<int64_t> plen(passes.size(), 0);
@@ -449,7 +468,7 @@ size_t batch_job_bytes(const accrqa_gb300_series_job &J) {
 Accrqa_Error check_batch_job(const accrqa_gb300_series_job &j) { return check_job(j); }
 
 Accrqa_Error run_batch_in(Context &c, const accrqa_gb300_series_job *jobs, int njobs,
-                          size_t budget) {
+                          size_t budget, const ResidentSeries *rs) {
     Accrqa_Error err = SUCCESS;
     int j0 = 0;
     while (j0 < njobs) {
@@ -461,7 +480,7 @@ Accrqa_Error run_batch_in(Context &c, const accrqa_gb300_series_job *jobs, int n
             need += b;
             j1++;
         }
-        if ((err = run_batch_part(c, jobs, j0, j1))) return err;
+        if ((err = run_batch_part(c, jobs, j0, j1, rs))) return err;
         j0 = j1;
     }
     return SUCCESS;

@@ -259,6 +259,12 @@ class Server:
         self._lib.accrqa_gb300_server_stats(self._h, ctypes.byref(b), ctypes.byref(s))
         return int(b.value), int(s.value)
 
+    def peak_bytes(self) -> int:
+        """Most device bytes the admitted requests held at once."""
+        self._lib.accrqa_gb300_server_peak_bytes.restype = ctypes.c_uint64
+        self._lib.accrqa_gb300_server_peak_bytes.argtypes = [ctypes.c_void_p]
+        return int(self._lib.accrqa_gb300_server_peak_bytes(self._h))
+
     def close(self):
         if self._h:
             self._lib.accrqa_gb300_server_destroy(self._h)

@@ -63,14 +63,13 @@ def cells_per_step(measures=3):
     return tot * measures
 
 
-# DRAM bytes (read + write) per launch of the dominant kernel, lam_rows, on
-# this workload: the mean over the 12 launches of one step in an ncu capture
-# (dram__bytes_read.sum + dram__bytes_write.sum).  Reads are the series (0.8
-# MB, L2-resident) and its re-reads, 8.6 MB; writes are the chunk boundary
-# records (13 chunks x 6250 bands x 16 slots x 32 lanes x lead and trail,
-# 333 MB, partly still in L2 at the end), 282 MB.  About 4.7 GB/s beside 11
-# TFLOP/s of algorithmic FP32 work: HBM is not the bound.
-LAM_TRAFFIC_PER_LAUNCH = 290_648_747
+# DRAM bytes (read + write) per pass of the dominant pass, LAM (tile_levels +
+# lam_levels), on this workload: the mean over the 12 passes of one step in an
+# ncu capture (dram__bytes_read.sum + dram__bytes_write.sum of both kernels).
+# tile_levels writes the level planes of the upper-triangle tiles (12.44 GB),
+# lam_levels reads them twice (24.87 GB) and writes the chunk records (0.33
+# GB).  5.5 ms of HBM time in a 39 ms pass: HBM is not the bound.
+LAM_TRAFFIC_PER_PASS = 37_662_000_000
 
 
 def algo_ops(nc, emb, nthr):
@@ -326,9 +325,13 @@ def run_ours(args):
                 "d2h_bytes_per_step": int(d2h.value // e2e_steps),
                 "path": "accrqa_gb300.RR/DET/LAM -> py_accrqa_* (host numpy buffers)"},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "fp32", "kernel": dom, "achieved": achieved / 1e12,
+        "roofline": {"bound": "fp32", "kernel": dom,
+                     "pass_kernels": {"rr": "rr_rows", "det": "det_diags + line_stitch",
+                                      "lam": "tile_levels + lam_levels + line_stitch"}[dom],
+                     "achieved": achieved / 1e12,
                      "peak": peak_ops / 1e12, "unit": "TFLOP/s",
-                     "frac": achieved / peak_ops, "traffic": LAM_TRAFFIC_PER_LAUNCH,
+                     "frac": achieved / peak_ops,
+                     "traffic": LAM_TRAFFIC_PER_PASS if dom == "lam" else None,
                      "peak_source": "measured: multiply/add chain probe "
                                     "(accrqa_gb300_probe_fp32), best of FP32 scalar and f32x2",
                      "probe_tflops": {k: v / 1e12 for k, v in probe.items()},
@@ -432,10 +435,20 @@ def batched_section(args):
 # ---------------------------------------------------------------------------
 # Served stream: Poisson arrivals, continuous batching vs sequential calls
 # ---------------------------------------------------------------------------
+_SERVED = {}
+
+
 def served_requests(count, seed=5):
     """Requests of the served stream: length log-uniform in [2000, 256000],
     float32 (float64 with probability 0.2), one measure of RR/DET/LAM, 1-16
-    thresholds (0.05-1.0 std), tau 1..4, emb 2..8, E/M norm."""
+    thresholds (0.05-1.0 std), tau 1..4, emb 2..8, E/M norm.  Generated once
+    per (count, seed); every rate serves the same requests."""
+    if (count, seed) not in _SERVED:
+        _SERVED[(count, seed)] = _make_served(count, seed)
+    return _SERVED[(count, seed)]
+
+
+def _make_served(count, seed):
     from accrqa_gb300 import workloads
     rng = np.random.default_rng(seed)
     gens = [workloads.logistic, workloads.ar1, workloads.white]
@@ -509,8 +522,9 @@ def served_section(args, rate):
             _, lat[done] = srv.wait(tickets[done])
             done += 1
         th.join()
-        t_served = time.perf_counter() - t0
+        t_served = time.perf_counter() - t0   # first arrival to last completion
         batches, served = srv.stats()
+        peak = srv.peak_bytes()
     # sequential plain calls, FIFO, same arrival times
     log("served: sequential plain calls")
     seq_lat = []
@@ -532,7 +546,11 @@ def served_section(args, rate):
     return {"workload": f"{len(reqs)} requests, Poisson {rate} req/s, n log-uniform "
                         "2e3..2.56e5, 20% fp64, one of RR/DET/LAM, 1-16 thresholds",
             "rate_req_s": rate, "workers": args.serve_workers, "batches": batches,
+            "arrival_span_s": float(arrivals[-1]),
+            "overloaded": bool(busy > arrivals[-1]),
+            "peak_admitted_bytes": int(peak),
             "value": cells / t_served, "unit": "cells/s",
+            "throughput": "cells over the makespan (first arrival to last completion)",
             "p50_ms": p(lat, 50), "p99_ms": p(lat, 99),
             "sequential_value": cells / t_seq, "sequential_p50_ms": p(seq_lat, 50),
             "sequential_p99_ms": p(seq_lat, 99), "seconds": t_served, "sequential_seconds": t_seq,
@@ -585,6 +603,7 @@ def cpu_baseline(budget_s):
     t0 = time.perf_counter()
     value, cells, cores = cpu_sample(budget_s)
     return {"value": value, "unit": "cells/s", "cores": cores, "kind": "port",
+            "estimate": "extrapolated",
             "sample": f"{cells:.3g} cells in {time.perf_counter() - t0:.1f}s: full N, tau=1, "
                       "1 threshold, row slices (RR, LAM) and diagonal slices (DET) for each "
                       "emb in {3,5,8}; cost per cell extrapolated to every (tau, emb, "
@@ -613,8 +632,11 @@ def run_reference(args):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "parallelism": "cpu"},
         "cpu_baseline": {"value": value, "unit": "cells/s", "cores": cores, "kind": "port",
-                         "sample": "per step: tau=1 emb=3 full N, 1 threshold, bounded "
-                                   "row/diagonal slices of RR, DET, LAM, extrapolated"},
+                         "estimate": "extrapolated",
+                         "sample": "per step: tau=1, emb in {3,5,8}, full N, 1 threshold, "
+                                   "bounded row (RR, LAM) and diagonal (DET) slices; the "
+                                   "measured cost per cell extrapolated to every (tau, emb, "
+                                   "threshold, measure) of the workload"},
         "e2e": {"value": value, "unit": "cells/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -761,8 +783,9 @@ def main(argv=None):
 
     ap.add_argument("--batch-series", type=int, default=512)
     ap.add_argument("--skip-served", action="store_true")
-    ap.add_argument("--serve-rates", type=lambda s: [float(v) for v in s.split(",")], default=[20.0, 60.0, 120.0])
-    ap.add_argument("--serve-requests", type=int, default=120)
+    ap.add_argument("--serve-rates", type=lambda s: [float(v) for v in s.split(",")],
+                    default=[50.0, 200.0, 500.0, 2000.0])
+    ap.add_argument("--serve-requests", type=int, default=1000)
     ap.add_argument("--serve-workers", type=int, default=4)
     args = ap.parse_args(argv)
     if args.warmup < 3 and args.impl == "ours":

@@ -194,6 +194,14 @@ void accrqa_gb300_transfer_stats(uint64_t *h2d_bytes, uint64_t *d2h_bytes,
 /* Number of CUDA kernels the engine has launched since load. */
 uint64_t accrqa_gb300_kernel_launches(void);
 
+/* Testing hook: the next `count` device allocations the engine makes fail on
+ * the host with an out-of-memory error before reaching the driver (0
+ * cancels), so that callers can see how failures surface: the public calls
+ * return ERR_CUDA_NOT_ENOUGH_MEMORY with a message in
+ * accrqa_gb300_last_error(), a server request completes with that code.  No
+ * device memory is touched. */
+void accrqa_gb300_test_fail_allocations(int32_t count);
+
 /* Comparison keys the kernels use for `nthr` thresholds of dtype `dtype`
  * under norm `norm` (1 Euclidean, 2 maximal): keys[k] is the largest value
  * v >= +0 of the squared sum (Euclidean) or of the maximal distance for which
@@ -317,11 +325,15 @@ typedef struct accrqa_gb300_series_job {
 Accrqa_Error accrqa_gb300_batch(const accrqa_gb300_series_job *jobs, int32_t njobs);
 
 /* A request server with continuous batching (no counterpart in the
- * reference).  `workers` threads, each with its own stream set and device
- * arena, repeatedly take every queued request that fits their share of
- * hbm_fraction of the free device memory and run them as one batch, so
- * requests that arrive while others are on the GPU start as soon as a worker
- * frees up and batches overlap on the device.
+ * reference).  Requests are admitted in arrival order while their device
+ * bytes fit hbm_fraction of the device memory free at the moment of each
+ * decision; an admitted request's series is uploaded once and stays on the
+ * device until it completes.  `workers` threads, each with its own stream set
+ * and device arena, repeatedly take the admitted requests (up to one work
+ * quantum) and run them as one batch on their resident series, so requests
+ * that arrive while others are on the GPU start as soon as memory and a
+ * worker free up and batches overlap on the device.  A request too large for
+ * the server even alone completes with ERR_CUDA_NOT_ENOUGH_MEMORY.
  *   submit: copies the job's series and thresholds, returns a ticket >= 0 or
  *           -Accrqa_Error; results go to the job's output buffers, which must
  *           stay valid until the ticket is waited for.
@@ -334,6 +346,8 @@ accrqa_gb300_server *accrqa_gb300_server_create(int32_t workers, double hbm_frac
 int64_t accrqa_gb300_server_submit(accrqa_gb300_server *s, const accrqa_gb300_series_job *job);
 Accrqa_Error accrqa_gb300_server_wait(accrqa_gb300_server *s, int64_t ticket, double *latency_ms);
 void accrqa_gb300_server_stats(accrqa_gb300_server *s, uint64_t *batches, uint64_t *served);
+/* Most device bytes the server's admitted requests held at once. */
+uint64_t accrqa_gb300_server_peak_bytes(accrqa_gb300_server *s);
 void accrqa_gb300_server_destroy(accrqa_gb300_server *s);
 
 /* The bit-packed recurrence plot of a device-resident series (>= n + 128

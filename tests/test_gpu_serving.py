@@ -73,3 +73,20 @@ def test_server_rejects_invalid_job(gpu):
                    thresholds=np.array([0.1], np.float32))
         with pytest.raises(engine.EngineError):
             srv.submit(bad)
+
+
+def test_burst_is_batched_on_resident_series(gpu):
+    """Many small requests submitted at once: the workers take them in
+    batches (fewer batches than requests) on the series admitted to the
+    device, and every result equals the plain call's."""
+    reqs = _requests(23, 48)
+    for r in reqs:   # small series, so that several fit one work quantum
+        r["x"] = r["x"][:min(len(r["x"]), 1500)]
+    with engine.Server(workers=2) as srv:
+        tickets = [srv.submit(r) for r in reqs]
+        results = [srv.wait(t) for t in tickets]
+        batches, served = srv.stats()
+    assert served == len(reqs)
+    assert batches < served
+    for j, (o, _) in zip(reqs, results):
+        np.testing.assert_array_equal(o[j["measures"][0]], _alone(j))

@@ -75,6 +75,12 @@ typedef struct accrqa_walk_desc {
      * results, a fraction of the distance work. */
     void *d_planes;
     int64_t planes_bytes;
+    /* with d_planes: nonzero when the planes already hold this pass's levels
+     * (an earlier DET or LAM pass of the same series, tau, emb, norm and
+     * thresholds wrote them): the pass walks its lines without storing them
+     * again */
+    int32_t planes_ready;
+    int32_t pad_;
 } accrqa_walk_desc;
 
 /* Enqueue one pass on `stream` (a cudaStream_t, 0 = legacy default stream).

@@ -4,8 +4,13 @@
 // thresholds.  The batch is planned on the host:
 //   1. all series go into one device arena with one host-to-device copy from
 //      pinned staging;
-//   2. each (series, measure, 16-threshold chunk) becomes a pass descriptor;
-//      passes are grouped by kernel shape (measure, dtype, norm, emb, slots);
+//   2. each (series, measure, 16-threshold chunk) becomes a pass descriptor
+//      (a series that wants LAM takes its RR from the LAM histograms: every
+//      recurrent cell lies on exactly one vertical line); passes are grouped
+//      by kernel shape (measure, dtype, norm, emb, slots).  A large series
+//      that wants LAM instead walks its chunked level passes of its own: the
+//      levels of its upper-triangle tiles stored once, LAM and DET walked
+//      from them (each unordered pair evaluated once for all three measures);
 //   3. each group's work units (bands or band pairs of all its series) are
 //      split into one contiguous range per resident warp with equal cells;
 //   4. the groups run concurrently on side streams, captured into one CUDA
@@ -68,9 +73,26 @@ struct Pass {
     int kind;
     int k0, cnt;
     int64_t nc;
+    bool levels = false;          // walked by the series' own level passes
+    bool rr_from_lines = false;   // LAM pass that also gives the series' RR
     size_t counts_off = 0, maxlen_off = 0, hist_off = 0;   // arena byte offsets
     accrqa_batch_job desc;
 };
+
+// Series at least this long (embedded) walk their DET/LAM from tile levels
+// in chunked per-series passes; shorter ones share the batched launches.
+constexpr int64_t kLevelNc = 16384;
+
+// One level unit: the LAM pass (and the DET pass, if wanted) of one series and
+// 16-threshold chunk, on one side stream with that stream's planes/records.
+struct LevelUnit {
+    int lam = -1, det = -1;   // pass indices
+    int stream = 0;
+    accrqa_walk_desc lam_d, det_d;
+};
+
+// never-recurrent keys of padding slots
+uint64_t never_key(int dtype) { return dtype == ACCRQA_GB300_F32 ? 0xBF800000ull : 0ull; }
 
 // (kind, dtype, norm, emb key, slots)
 typedef std::tuple<int, int, int, int, int> GroupKey;
@@ -146,15 +168,20 @@ static Accrqa_Error run_batch_part(Context &c, const accrqa_gb300_series_job *jo
         const accrqa_gb300_series_job &J = jobs[j];
         const int kinds[3] = {ACCRQA_WALK_RR, ACCRQA_WALK_DET, ACCRQA_WALK_LAM};
         void *outs[3] = {J.rr_out, J.det_out, J.lam_out};
+        const int64_t nc = J.n - (int64_t)(J.emb - 1) * J.tau;
+        const bool big = J.lam_out && nc >= kLevelNc;
         for (int q = 0; q < 3; q++) {
             if (!outs[q]) continue;
+            if (q == 0 && J.lam_out) continue;   // RR from the LAM histograms
             for (int k0 = 0; k0 < J.nthr; k0 += ACCRQA_MAX_THR_PER_PASS) {
                 Pass p;
                 p.job = j;
                 p.kind = kinds[q];
                 p.k0 = k0;
                 p.cnt = std::min(J.nthr - k0, ACCRQA_MAX_THR_PER_PASS);
-                p.nc = J.n - (int64_t)(J.emb - 1) * J.tau;
+                p.nc = nc;
+                p.levels = big;
+                p.rr_from_lines = q == 2 && J.rr_out != nullptr;
                 passes.push_back(p);
             }
         }
@@ -185,8 +212,14 @@ static Accrqa_Error run_batch_part(Context &c, const accrqa_gb300_series_job *jo
     const size_t zero_end = off;
 
     std::map<GroupKey, std::vector<int>> groups;
+    std::map<std::pair<int, int>, LevelUnit> level_map;   // (job, k0) -> unit
     for (int i = 0; i < (int)passes.size(); i++) {
         const Pass &p = passes[(size_t)i];
+        if (p.levels) {
+            LevelUnit &u = level_map[std::make_pair(p.job, p.k0)];
+            (p.kind == ACCRQA_WALK_LAM ? u.lam : u.det) = i;
+            continue;
+        }
         const accrqa_gb300_series_job &J = jobs[p.job];
         const int nt = p.cnt <= 8 ? 8 : 16;
         const int dt = maxabs[(size_t)(p.job - j0)] >= 0.0 ? ACCRQA_F64F : J.dtype;
@@ -287,14 +320,73 @@ static Accrqa_Error run_batch_part(Context &c, const accrqa_gb300_series_job *jo
         for (int pi_i = 0; pi_i < (int)g.second.size(); pi_i++) gp.table[(size_t)pi_i].pad_ = g.second[(size_t)pi_i];
         plans.push_back(std::move(gp));
     }
+    const size_t upload_end = align16(off);   // tables end here
+
+    // Level units: descriptors, then side streams by cost (largest first to
+    // the least loaded), each stream with planes and chunk records for the
+    // largest of its units (its units run one after another).
+    std::vector<LevelUnit> levels;
+    for (auto &kv : level_map) levels.push_back(kv.second);
+    for (LevelUnit &u : levels) {
+        for (int which = 0; which < 2; which++) {
+            const int pi = which == 0 ? u.lam : u.det;
+            if (pi < 0) continue;
+            const Pass &p = passes[(size_t)pi];
+            const accrqa_gb300_series_job &J = jobs[p.job];
+            accrqa_walk_desc &d = which == 0 ? u.lam_d : u.det_d;
+            std::memset(&d, 0, sizeof(d));
+            d.kind = p.kind;
+            d.dtype = J.dtype == ACCRQA_GB300_F32 ? ACCRQA_F32 : ACCRQA_F64;
+            d.norm = J.norm;
+            d.tau = J.tau;
+            d.emb = J.emb;
+            d.nthr = p.cnt;
+            d.nc = p.nc;
+            for (int k = 0; k < ACCRQA_MAX_THR_PER_PASS; k++)
+                d.keys[k] = k < p.cnt ? (J.dtype == ACCRQA_GB300_F32
+                                             ? key_of<float>(J.thresholds, p.k0 + k, J.norm)
+                                             : key_of<double>(J.thresholds, p.k0 + k, J.norm))
+                                      : never_key(J.dtype);
+            const double m = maxabs[(size_t)(p.job - j0)];
+            if (m >= 0.0)
+                for (int k = 0; k < ACCRQA_MAX_THR_PER_PASS; k++)
+                    d.filter_keys[k] = f64_filter_pair(d.keys[k], J.norm, J.emb, m);
+            d.hist_stride = p.nc + 1;
+        }
+    }
+    std::sort(levels.begin(), levels.end(), [&](const LevelUnit &a, const LevelUnit &b) {
+        const Pass &pa = passes[(size_t)a.lam], &pb = passes[(size_t)b.lam];
+        return pa.nc * pa.nc * pa.cnt > pb.nc * pb.nc * pb.cnt;
+    });
+    std::vector<double> load(kSideStreams, 0.0);
+    std::vector<int64_t> s_planes(kSideStreams, 0), s_records(kSideStreams, 0);
+    for (LevelUnit &u : levels) {
+        const int st = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        u.stream = st;
+        const Pass &pl = passes[(size_t)u.lam];
+        load[(size_t)st] += (double)pl.nc * (double)pl.nc * pl.cnt * (u.det >= 0 ? 1.5 : 1.0);
+        s_planes[(size_t)st] =
+            std::max(s_planes[(size_t)st], accrqa_gb300_walk_plane_bytes(&u.lam_d));
+        int64_t rec = accrqa_gb300_walk_scratch_bytes(&u.lam_d);
+        if (u.det >= 0) rec = std::max(rec, accrqa_gb300_walk_scratch_bytes(&u.det_d));
+        s_records[(size_t)st] = std::max(s_records[(size_t)st], rec);
+    }
+    // per-stream planes and records last: neither uploaded nor zeroed
+    std::vector<size_t> planes_off(kSideStreams, 0), records_off(kSideStreams, 0);
+    off = upload_end;
+    for (int st = 0; st < kSideStreams; st++) {
+        planes_off[(size_t)st] = align16(off);
+        off = planes_off[(size_t)st] + (size_t)s_planes[(size_t)st];
+        records_off[(size_t)st] = align16(off);
+        off = records_off[(size_t)st] + (size_t)s_records[(size_t)st];
+    }
     const size_t arena_bytes = align16(off);
 
+    // ---- stage ------------------------------------------------------------
     trace("batch [%d, %d): %zu passes, %zu groups planned, arena %zu MB", j0, j1,
           passes.size(), plans.size(), arena_bytes >> 20);
-    // ---- stage ------------------------------------------------------------
     CUB(c.arena.reserve(arena_bytes), "cudaMalloc(batch arena)");
     char *dev = (char *)c.arena.ptr;
-    const size_t upload_end = arena_bytes;
     CUB(pinned_reserve(c, upload_end), "cudaHostAlloc(batch staging)");
     char *host = (char *)c.pinned;
     for (int j = j0; j < j1; j++) {
@@ -346,10 +438,40 @@ static Accrqa_Error run_batch_part(Context &c, const accrqa_gb300_series_job *jo
     if (series_bytes)
         CUB(cudaMemcpyAsync(dev, host, series_bytes, cudaMemcpyHostToDevice, c.stream),
             "cudaMemcpy(batch series)");
-    if (arena_bytes > zero_end)
-        CUB(cudaMemcpyAsync(dev + zero_end, host + zero_end, arena_bytes - zero_end,
+    if (upload_end > zero_end)
+        CUB(cudaMemcpyAsync(dev + zero_end, host + zero_end, upload_end - zero_end,
                             cudaMemcpyHostToDevice, c.stream), "cudaMemcpy(batch tables)");
-    transfer_stats_add(series_bytes + (arena_bytes - zero_end), 0);
+    transfer_stats_add(series_bytes + (upload_end - zero_end), 0);
+    // the level units' device pointers
+    for (LevelUnit &u : levels) {
+        for (int which = 0; which < 2; which++) {
+            const int pi = which == 0 ? u.lam : u.det;
+            if (pi < 0) continue;
+            const Pass &p = passes[(size_t)pi];
+            accrqa_walk_desc &d = which == 0 ? u.lam_d : u.det_d;
+            if (resident(p.job)) {
+                d.d_x = rs[p.job].x;
+                if (maxabs[(size_t)(p.job - j0)] >= 0.0) {
+                    d.d_xhi = rs[p.job].hi;
+                    d.d_xlo = rs[p.job].lo;
+                }
+            } else {
+                d.d_x = dev + xoff[(size_t)(p.job - j0)];
+                if (maxabs[(size_t)(p.job - j0)] >= 0.0) {
+                    const size_t ho = hioff[(size_t)(p.job - j0)];
+                    d.d_xhi = dev + ho;
+                    d.d_xlo = (const float *)(dev + ho) + (jobs[p.job].n + ACCRQA_SERIES_PAD);
+                }
+            }
+            d.d_hist = (uint64_t *)(dev + p.hist_off);
+            d.d_maxlen = (uint32_t *)(dev + p.maxlen_off);
+            d.d_scratch = s_records[(size_t)u.stream] ? dev + records_off[(size_t)u.stream] : nullptr;
+            d.scratch_bytes = s_records[(size_t)u.stream];
+            d.d_planes = dev + planes_off[(size_t)u.stream];
+            d.planes_bytes = s_planes[(size_t)u.stream];
+            d.planes_ready = which == 1 ? 1 : 0;   // DET after the LAM pass stored them
+        }
+    }
     CUB(cudaMemsetAsync(dev + zero_begin, 0, zero_end - zero_begin, c.stream), "cudaMemset(batch)");
 
     // ---- launch: every group on a side stream, captured as one graph ------
@@ -364,7 +486,8 @@ static Accrqa_Error run_batch_part(Context &c, const accrqa_gb300_series_job *jo
     cudaError_t ce = cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal);
     if (ce == cudaSuccess) {
         cudaEventRecord(fork, c.stream);
-        const int ns = std::min<int>(kSideStreams, (int)plans.size());
+        const int ns = std::max(std::min<int>(kSideStreams, (int)plans.size()),
+                                levels.empty() ? 0 : kSideStreams);
         for (int s = 0; s < ns; s++) cudaStreamWaitEvent(c.side[(size_t)s], fork, 0);
         // largest groups first, round-robin over the side streams
         std::vector<int> ord(plans.size());
@@ -375,6 +498,14 @@ static Accrqa_Error run_batch_part(Context &c, const accrqa_gb300_series_job *jo
         for (size_t i = 0; i < ord.size(); i++) {
             const int e = accrqa_gb300_launch_batch(&plans[(size_t)ord[i]].L, c.side[i % (size_t)ns]);
             if (e && err == SUCCESS) err = cuda_error((cudaError_t)e, "batched kernel launch");
+        }
+        // the large series' level passes: LAM (stores the levels), then DET
+        // from them, on the unit's side stream
+        for (LevelUnit &u : levels) {
+            cudaStream_t st = c.side[(size_t)u.stream];
+            int e = accrqa_gb300_launch_walk(&u.lam_d, st);
+            if (!e && u.det >= 0) e = accrqa_gb300_launch_walk(&u.det_d, st);
+            if (e && err == SUCCESS) err = cuda_error((cudaError_t)e, "level pass launch");
         }
         for (int s = 0; s < ns; s++) {
             cudaEventRecord(join[s], c.side[(size_t)s]);
@@ -409,7 +540,9 @@ static Accrqa_Error run_batch_part(Context &c, const accrqa_gb300_series_job *jo
         const uint32_t *mx = (const uint32_t *)(small.data() + (p.maxlen_off - zero_begin));
         uint32_t m = 0;
         for (int k = 0; k < p.cnt; k++) m = std::max(m, mx[k]);
-        int64_t P = std::max<int64_t>((int64_t)m + 1, ACCRQA_BATCH_BINS);
+        // runs below the kernels' short bins leave no longest-run marker
+        int64_t P = std::max<int64_t>((int64_t)m + 1,
+                                      p.levels ? ACCRQA_SHORT_RUN_BINS : ACCRQA_BATCH_BINS);
         P = std::min<int64_t>(P, p.nc + 1);
         plen[i] = P;
         pref[i].resize((size_t)P * p.cnt);
@@ -446,6 +579,12 @@ static Accrqa_Error run_batch_part(Context &c, const accrqa_gb300_series_job *jo
                 else last = 1;
             }
             LineHistogram lh(std::move(h), last, p.nc);
+            if (p.rr_from_lines) {
+                // sum of l * H[l] over the vertical lines = recurrent cells
+                const double rr = (double)lh.metric(0) / (double)(p.nc * p.nc);
+                if (f32) ((float *)J.rr_out)[p.k0 + k] = (float)rr;
+                else ((double *)J.rr_out)[p.k0 + k] = rr;
+            }
             void *out = is_det ? J.det_out : J.lam_out;
             if (f32) write_line_out<float>(out, p.k0 + k, lh, lm, full, is_det);
             else write_line_out<double>(out, p.k0 + k, lh, lm, full, is_det);
@@ -462,6 +601,11 @@ size_t batch_job_bytes(const accrqa_gb300_series_job &J) {
     const int lines = (J.det_out ? 1 : 0) + (J.lam_out ? 1 : 0);
     b += (size_t)lines * (size_t)J.nthr * (size_t)(nc + 1) * 8;
     b += (size_t)(nc / 32 + 2) * 16;   // units
+    if (J.lam_out && nc >= kLevelNc) {
+        // tile levels (up to 5 planes of 128 bytes per 32x32 tile) and chunk records
+        const int64_t T = (nc + 31) / 32;
+        b += (size_t)(T * (T + 1) / 2) * 5 * 128 + (size_t)T * 2 * 4096;
+    }
     return b;
 }
 

@@ -124,9 +124,10 @@ static int grid_for(long long units, int per_sm) {
 }
 
 // The level walk of one DET/LAM pass (rqa_planes.cuh): tile_levels stores
-// the levels of the upper-triangle tiles to d.d_planes, then det_levels or
-// lam_levels walks the lines from them in lam_rows' / det_diags' units, and
-// the stitch joins the chunks -- all on `st`, in that order.
+// the levels of the upper-triangle tiles to d.d_planes (unless an earlier
+// pass left them there: d.planes_ready), then det_levels or lam_levels walks
+// the lines from them in lam_rows' / det_diags' units, and the stitch joins
+// the chunks -- all on `st`, in that order.
 template <typename T, int NORM, int EMB, int NT>
 static cudaError_t launch_levels_one(const accrqa_walk_desc &d, cudaStream_t st) {
     constexpr int NP = Planes<NT>::kN;
@@ -148,11 +149,13 @@ static cudaError_t launch_levels_one(const accrqa_walk_desc &d, cudaStream_t st)
     e = per_sm_of(walk, LineSmem<NT>::kBytes, det ? c_det : c_lam, &per2);
     if (e != cudaSuccess) return e;
 
-    plan_upper_units(T_, (long long)sm_count_cached() * per1 * kWarpsPerCta, &a.chunk,
-                     &a.nunits);
-    tile_levels<T, NORM, EMB, NT><<<grid_for(a.nunits, per1), kWarpsPerCta * 32, 0, st>>>(a);
-    g_launches.fetch_add(1);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (!d.planes_ready) {
+        plan_upper_units(T_, (long long)sm_count_cached() * per1 * kWarpsPerCta, &a.chunk,
+                         &a.nunits);
+        tile_levels<T, NORM, EMB, NT><<<grid_for(a.nunits, per1), kWarpsPerCta * 32, 0, st>>>(a);
+        g_launches.fetch_add(1);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
 
     // chunked when the caller's scratch holds the boundary records
     LinePlan q = plan_lines(det, d.nc, sm_count_cached(), d.d_scratch != nullptr);

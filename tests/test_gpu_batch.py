@@ -100,3 +100,38 @@ def test_batch_rejects_bad_job(gpu):
     jobs[1]["tau"] = 0
     with pytest.raises(engine.EngineError):
         engine.batch(jobs)
+
+
+def test_batch_large_series_from_tile_levels(gpu):
+    """Series long enough for the level passes (their DET and LAM walked from
+    one store of tile levels, their RR taken from the LAM histograms) mixed
+    with short ones: every output equals the plain calls', bit for bit."""
+    rng = np.random.default_rng(31)
+    jobs = []
+    for i, n in enumerate([17000, 23000, 1200, 30000, 2500, 19000]):
+        dt = np.float64 if i % 3 == 2 or i == 5 else np.float32
+        x = workloads.lorenz_x(n, 100 + i, transient=500).astype(dt)
+        x = (x / np.std(x.astype(np.float64))).astype(dt)
+        nthr = [3, 8, 11, 20, 5, 16][i]
+        jobs.append(dict(x=x, tau=int(rng.integers(1, 4)), emb=int(rng.integers(2, 7)),
+                         norm=1 + i % 2,
+                         thresholds=np.sort(rng.uniform(0.05, 1.0, nthr)).astype(dt),
+                         lmin=2, vmin=2, calc_entr=1 - (i == 3)))
+    for measures in (("rr", "det", "lam"), ("rr", "lam"), ("det", "lam")):
+        outs = engine.batch(jobs, measures=measures)
+        for j, o in zip(jobs, outs):
+            D = A.accrqaDistance("euclidean" if j["norm"] == 1 else "maximal")
+            t = np.array([j["tau"]], np.intc)
+            e = np.array([j["emb"]], np.intc)
+            if "rr" in measures:
+                np.testing.assert_array_equal(
+                    o["rr"], A.RR(j["x"], t, e, j["thresholds"], D, tidy_data=False).reshape(-1))
+            if "det" in measures:
+                np.testing.assert_array_equal(
+                    o["det"], A.DET(j["x"], t, e, np.array([2], np.intc), j["thresholds"], D,
+                                    calculate_ENTR=bool(j["calc_entr"]),
+                                    tidy_data=False).reshape(-1, 5))
+            np.testing.assert_array_equal(
+                o["lam"], A.LAM(j["x"], t, e, np.array([2], np.intc), j["thresholds"], D,
+                                calculate_ENTR=bool(j["calc_entr"]),
+                                tidy_data=False).reshape(-1, 5))

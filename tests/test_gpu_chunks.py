@@ -39,10 +39,12 @@ class WalkDesc(ctypes.Structure):
         ("filter_keys", ctypes.c_uint64 * MAX_THR),
         ("d_scratch", ctypes.c_void_p), ("scratch_bytes", ctypes.c_int64),
         ("d_planes", ctypes.c_void_p), ("planes_bytes", ctypes.c_int64),
+        ("planes_ready", ctypes.c_int32), ("pad_", ctypes.c_int32),
     ]
 
 
-def _walk(torch, lib, kind, dx, dt, n, tau, emb, thr, norm, chunked, levels=False):
+def _walk(torch, lib, kind, dx, dt, n, tau, emb, thr, norm, chunked, levels=False,
+          planes=None, ready=False):
     nc = n - (emb - 1) * tau
     keys = engine.threshold_keys(thr, dt, norm)
     hist = torch.zeros((len(thr), nc + 1), dtype=torch.int64, device="cuda")
@@ -60,12 +62,13 @@ def _walk(torch, lib, kind, dx, dt, n, tau, emb, thr, norm, chunked, levels=Fals
         assert want > 0, "this size must chunk"
         scratch = torch.empty(want, dtype=torch.uint8, device="cuda")
         d.d_scratch, d.scratch_bytes = scratch.data_ptr(), want
-    planes = None
     if levels:
         pb = lib.accrqa_gb300_walk_plane_bytes(ctypes.byref(d))
         assert pb > 0
-        planes = torch.empty(pb, dtype=torch.uint8, device="cuda")
+        if planes is None:
+            planes = torch.empty(pb, dtype=torch.uint8, device="cuda")
         d.d_planes, d.planes_bytes = planes.data_ptr(), pb
+        d.planes_ready = 1 if ready else 0
     st = torch.cuda.current_stream().cuda_stream
     assert lib.accrqa_gb300_launch_walk(ctypes.byref(d), ctypes.c_void_p(st)) == 0
     torch.cuda.synchronize()
@@ -124,3 +127,33 @@ def test_levels_equal_distance_walk(kind, dt, nthr, n, tau, emb, norm):
         h1, m1 = _walk(torch, lib, kind, dx, dt, n, tau, emb, thr, norm, chunked=ch, levels=True)
         np.testing.assert_array_equal(h1, h0)
         np.testing.assert_array_equal(m1, m0)
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+@pytest.mark.parametrize("n,tau,emb,norm", [(20000, 1, 3, 1), (4096, 3, 4, 2), (97, 1, 2, 1)])
+def test_det_from_planes_a_lam_pass_left(dt, n, tau, emb, norm):
+    """A DET pass given the planes an earlier LAM pass of the same series
+    stored (planes_ready) skips the tile walk and still equals the distance
+    walk."""
+    torch = pytest.importorskip("torch")
+    lib = _lib.handle()
+    _bind(lib)
+    x = workloads.logistic(n, 13 + n).astype(dt)
+    thr = np.array([0.0, 0.05, 0.1, 0.3, 0.8, 4.0], dtype=dt)
+    dx = torch.zeros(n + 128, dtype=torch.float32 if dt == np.float32 else torch.float64,
+                     device="cuda")
+    dx[:n] = torch.from_numpy(x).cuda()
+    d = WalkDesc()
+    d.kind, d.nc, d.nthr = WALK_LAM, n - (emb - 1) * tau, len(thr)
+    planes = torch.empty(lib.accrqa_gb300_walk_plane_bytes(ctypes.byref(d)), dtype=torch.uint8,
+                         device="cuda")
+    ch = n >= 3000
+    hl, _ = _walk(torch, lib, WALK_LAM, dx, dt, n, tau, emb, thr, norm, chunked=ch,
+                  levels=True, planes=planes)
+    hd, md = _walk(torch, lib, WALK_DET, dx, dt, n, tau, emb, thr, norm, chunked=ch,
+                   levels=True, planes=planes, ready=True)
+    h0, m0 = _walk(torch, lib, WALK_DET, dx, dt, n, tau, emb, thr, norm, chunked=False)
+    np.testing.assert_array_equal(hd, h0)
+    np.testing.assert_array_equal(md, m0)
+    h1, _ = _walk(torch, lib, WALK_LAM, dx, dt, n, tau, emb, thr, norm, chunked=False)
+    np.testing.assert_array_equal(hl, h1)

@@ -4,7 +4,7 @@
 #include <cmath>
 #include <cstdio>
 
-#include "../../include/accrqa_gb300.hpp"
+#include "accrqa_gb300.hpp"
 #include "engine.hpp"
 
 using namespace accrqa;

@@ -6,7 +6,7 @@
 // same on top of this library.
 #include <cstdio>
 
-#include "../../include/accrqa_gb300.hpp"
+#include "accrqa_gb300.hpp"
 
 namespace {
 

@@ -12,7 +12,7 @@
 #include <mutex>
 #include <vector>
 
-#include "../../include/accrqa_gb300.h"
+#include "accrqa_gb300.h"
 #include "engine_abi.h"
 
 namespace accrqa {

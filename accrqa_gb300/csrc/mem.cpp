@@ -9,7 +9,7 @@
 #include <cstdlib>
 #include <cstring>
 
-#include "../../include/accrqa_gb300.h"
+#include "accrqa_gb300.h"
 
 struct Mem {
     MemType type;

@@ -19,7 +19,7 @@
 #include <cstdint>
 #include <mutex>
 
-#include "../../include/accrqa_gb300.h"
+#include "accrqa_gb300.h"
 #include "engine_abi.h"
 #include "rqa_device.cuh"
 

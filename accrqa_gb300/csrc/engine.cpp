@@ -712,7 +712,7 @@ static Accrqa_Error fetch_histograms(Context &c, int kind, const uint64_t *d_his
     CU(c.pair_count.reserve(8), "cudaMalloc(pair count)");
     CU(cudaMemsetAsync(c.pair_count.ptr, 0, 8, c.stream), "cudaMemset(pair count)");
     int e = accrqa_gb300_launch_compact(d_hist, stride, nthr, p, (uint64_t *)c.pairs.ptr, cap,
-                                        (unsigned long long *)c.pair_count.ptr, c.stream);
+                                        (unsigned long long *)c.pair_count.ptr, 0, c.stream);
     if (e) return cuda_error((cudaError_t)e, "histogram compaction");
     unsigned long long total = 0;
     CU(copy_async(&total, c.pair_count.ptr, 8, cudaMemcpyDeviceToHost, c.stream),

@@ -186,8 +186,11 @@ Accrqa_Error run_batch(const accrqa_gb300_series_job *jobs, int njobs);
 // uploading its x (c.stream must be ordered after those uploads).
 Accrqa_Error run_batch_in(Context &c, const accrqa_gb300_series_job *jobs, int njobs,
                           size_t budget, const ResidentSeries *rs = nullptr);
-// Device bytes one job of a batch needs (series, histograms, work units).
+// Device bytes one job of a batch needs (series, histograms, work units), and
+// the tile levels and chunk records of its level passes (0 for a job without
+// them; a batch holds these once per side stream, for its largest job).
 size_t batch_job_bytes(const accrqa_gb300_series_job &job);
+size_t batch_job_level_bytes(const accrqa_gb300_series_job &job);
 Accrqa_Error check_batch_job(const accrqa_gb300_series_job &job);
 // A context that is not the device's shared one (for server workers).
 Context *context_create(Accrqa_Error *err);

@@ -109,12 +109,13 @@ int accrqa_gb300_launch_rp_bits(const void *d_x, int32_t dtype, int32_t norm,
                                 void *d_out, int64_t row0, int64_t nrows, void *stream);
 
 /* The non-zero bins of nthr histogram rows (bins [0, p), row stride
- * `stride`) as pairs {(row << 40) | length, count}, in no particular order;
- * *d_count (zeroed by the caller) receives their number.  Pairs past `cap`
- * are counted, not written. */
+ * `stride`) as pairs {((row0 + row) << 40) | length, count}, in no particular
+ * order, appended to d_pairs; *d_count (zeroed by the caller before the
+ * first of a series of calls) receives their number.  Pairs past `cap` are
+ * counted, not written. */
 int accrqa_gb300_launch_compact(const uint64_t *d_hist, int64_t stride, int32_t nthr,
                                 int64_t p, uint64_t *d_pairs, int64_t cap,
-                                unsigned long long *d_count, void *stream);
+                                unsigned long long *d_count, int64_t row0, void *stream);
 
 /* Number of streaming multiprocessors of the current device (cached). */
 int accrqa_gb300_sm_count(void);

@@ -24,6 +24,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <tuple>
 #include <vector>
 
@@ -521,37 +522,84 @@ static Accrqa_Error run_batch_part(Context &c, const accrqa_gb300_series_job *jo
     for (int s = 0; s < kSideStreams; s++) cudaEventDestroy(join[s]);
     if (err != SUCCESS) return err;
     CUB(ce, "batch graph");
+    trace("batch: graph launched");
 
     // ---- results ----------------------------------------------------------
+    // The line passes' non-zero bins, compacted on the device (row = pass * 16
+    // + slot): only those come back, not the dense histogram prefixes.
+    int64_t total_bins = 0;
+    for (const Pass &p : passes)
+        if (p.kind != ACCRQA_WALK_RR) total_bins += (int64_t)p.cnt * (p.nc + 1);
+    const int64_t cap = std::max<int64_t>(65536, total_bins / 4);
+    bool compacted = total_bins > 0;
+    if (compacted) {
+        CUB(c.pairs.reserve((size_t)cap * 16), "cudaMalloc(histogram pairs)");
+        CUB(c.pair_count.reserve(8), "cudaMalloc(pair count)");
+        CUB(cudaMemsetAsync(c.pair_count.ptr, 0, 8, c.stream), "cudaMemset(pair count)");
+        for (size_t i = 0; i < passes.size(); i++) {
+            const Pass &p = passes[i];
+            if (p.kind == ACCRQA_WALK_RR) continue;
+            const int e = accrqa_gb300_launch_compact(
+                (const uint64_t *)(dev + p.hist_off), p.nc + 1, p.cnt, p.nc + 1,
+                (uint64_t *)c.pairs.ptr, cap, (unsigned long long *)c.pair_count.ptr,
+                (int64_t)i * 16, c.stream);
+            if (e) return cuda_error((cudaError_t)e, "histogram compaction");
+        }
+    }
     std::vector<char> small(head_end - zero_begin);
     if (head_end > zero_begin) {
         CUB(cudaMemcpyAsync(small.data(), dev + zero_begin, head_end - zero_begin,
                             cudaMemcpyDeviceToHost, c.stream), "cudaMemcpy(batch counts)");
         transfer_stats_add(0, head_end - zero_begin);
     }
+    unsigned long long npairs = 0;
+    if (compacted) {
+        CUB(cudaMemcpyAsync(&npairs, c.pair_count.ptr, 8, cudaMemcpyDeviceToHost, c.stream),
+            "cudaMemcpy(pair count)");
+        transfer_stats_add(0, 8);
+    }
     CUB(cudaStreamSynchronize(c.stream), "batched kernels");
-    trace("batch: kernels done");
-    // histogram prefixes
+    trace("batch: kernels done, %llu non-zero bins", npairs);
+    compacted = compacted && (int64_t)npairs <= cap;
+    // sparse bins per (pass, slot) when compacted, else dense prefixes
+    std::vector<std::vector<std::pair<int64_t, uint64_t>>> bins;
     std::vector<std::vector<uint64_t>> pref(passes.size());
     std::vector<int64_t> plen(passes.size(), 0);
-    for (size_t i = 0; i < passes.size(); i++) {
-        const Pass &p = passes[i];
-        if (p.kind == ACCRQA_WALK_RR) continue;
-        const uint32_t *mx = (const uint32_t *)(small.data() + (p.maxlen_off - zero_begin));
-        uint32_t m = 0;
-        for (int k = 0; k < p.cnt; k++) m = std::max(m, mx[k]);
-        // runs below the kernels' short bins leave no longest-run marker
-        int64_t P = std::max<int64_t>((int64_t)m + 1,
-                                      p.levels ? ACCRQA_SHORT_RUN_BINS : ACCRQA_BATCH_BINS);
-        P = std::min<int64_t>(P, p.nc + 1);
-        plen[i] = P;
-        pref[i].resize((size_t)P * p.cnt);
-        CUB(cudaMemcpy2DAsync(pref[i].data(), (size_t)P * 8, dev + p.hist_off, (size_t)(p.nc + 1) * 8,
-                              (size_t)P * 8, (size_t)p.cnt, cudaMemcpyDeviceToHost, c.stream),
-            "cudaMemcpy(batch histograms)");
-        transfer_stats_add(0, (size_t)P * 8 * p.cnt);
+    if (compacted) {
+        std::vector<uint64_t> pr((size_t)npairs * 2);
+        if (npairs)
+            CUB(cudaMemcpyAsync(pr.data(), c.pairs.ptr, (size_t)npairs * 16,
+                                cudaMemcpyDeviceToHost, c.stream), "cudaMemcpy(histogram pairs)");
+        transfer_stats_add(0, (size_t)npairs * 16);
+        CUB(cudaStreamSynchronize(c.stream), "histogram copy");
+        bins.resize(passes.size() * 16);
+        for (size_t t = 0; t < (size_t)npairs; t++) {
+            const uint64_t key = pr[2 * t];
+            bins[(size_t)(key >> 40)].emplace_back((int64_t)(key & ((1ull << 40) - 1)),
+                                                   pr[2 * t + 1]);
+        }
+    } else {
+        for (size_t i = 0; i < passes.size(); i++) {
+            const Pass &p = passes[i];
+            if (p.kind == ACCRQA_WALK_RR) continue;
+            const uint32_t *mx = (const uint32_t *)(small.data() + (p.maxlen_off - zero_begin));
+            uint32_t m = 0;
+            for (int k = 0; k < p.cnt; k++) m = std::max(m, mx[k]);
+            // runs below the kernels' short bins leave no longest-run marker
+            int64_t P = std::max<int64_t>((int64_t)m + 1,
+                                          p.levels ? ACCRQA_SHORT_RUN_BINS : ACCRQA_BATCH_BINS);
+            P = std::min<int64_t>(P, p.nc + 1);
+            plen[i] = P;
+            pref[i].resize((size_t)P * p.cnt);
+            CUB(cudaMemcpy2DAsync(pref[i].data(), (size_t)P * 8, dev + p.hist_off,
+                                  (size_t)(p.nc + 1) * 8, (size_t)P * 8, (size_t)p.cnt,
+                                  cudaMemcpyDeviceToHost, c.stream),
+                "cudaMemcpy(batch histograms)");
+            transfer_stats_add(0, (size_t)P * 8 * p.cnt);
+        }
+        CUB(cudaStreamSynchronize(c.stream), "histogram copy");
     }
-    CUB(cudaStreamSynchronize(c.stream), "histogram copy");
+    trace("batch: histograms fetched");
 
     for (size_t i = 0; i < passes.size(); i++) {
         const Pass &p = passes[i];
@@ -571,14 +619,30 @@ static Accrqa_Error run_batch_part(Context &c, const accrqa_gb300_series_job *jo
         const bool full = J.calc_entr == 1 || lm >= 16;
         const int64_t P = plen[i];
         for (int k = 0; k < p.cnt; k++) {
-            std::vector<uint64_t> h(pref[i].begin() + (size_t)k * P, pref[i].begin() + (size_t)(k + 1) * P);
-            uint64_t last = 0;
-            if (is_det) {
-                for (auto &v : h) v = 2 * v;
-                if (P == p.nc + 1) h[(size_t)p.nc] += 1;
-                else last = 1;
+            std::unique_ptr<LineHistogram> lhp;
+            if (compacted) {
+                // DET rows hold the raw upper-triangle runs: doubled, plus the
+                // line of identity (src/AccRQA_CPU_function.cpp:156-162)
+                auto &r = bins[i * 16 + (size_t)k];
+                std::sort(r.begin(), r.end());
+                if (is_det) {
+                    for (auto &b : r) b.second *= 2;
+                    if (!r.empty() && r.back().first == p.nc) r.back().second += 1;
+                    else r.emplace_back(p.nc, 1);
+                }
+                lhp.reset(new LineHistogram(std::move(r), p.nc));
+            } else {
+                std::vector<uint64_t> h(pref[i].begin() + (size_t)k * P,
+                                        pref[i].begin() + (size_t)(k + 1) * P);
+                uint64_t last = 0;
+                if (is_det) {
+                    for (auto &v : h) v = 2 * v;
+                    if (P == p.nc + 1) h[(size_t)p.nc] += 1;
+                    else last = 1;
+                }
+                lhp.reset(new LineHistogram(std::move(h), last, p.nc));
             }
-            LineHistogram lh(std::move(h), last, p.nc);
+            const LineHistogram &lh = *lhp;
             if (p.rr_from_lines) {
                 // sum of l * H[l] over the vertical lines = recurrent cells
                 const double rr = (double)lh.metric(0) / (double)(p.nc * p.nc);
@@ -590,6 +654,7 @@ static Accrqa_Error run_batch_part(Context &c, const accrqa_gb300_series_job *jo
             else write_line_out<double>(out, p.k0 + k, lh, lm, full, is_det);
         }
     }
+    trace("batch: measures written");
     return SUCCESS;
 }
 
@@ -601,12 +666,15 @@ size_t batch_job_bytes(const accrqa_gb300_series_job &J) {
     const int lines = (J.det_out ? 1 : 0) + (J.lam_out ? 1 : 0);
     b += (size_t)lines * (size_t)J.nthr * (size_t)(nc + 1) * 8;
     b += (size_t)(nc / 32 + 2) * 16;   // units
-    if (J.lam_out && nc >= kLevelNc) {
-        // tile levels (up to 5 planes of 128 bytes per 32x32 tile) and chunk records
-        const int64_t T = (nc + 31) / 32;
-        b += (size_t)(T * (T + 1) / 2) * 5 * 128 + (size_t)T * 2 * 4096;
-    }
     return b;
+}
+
+size_t batch_job_level_bytes(const accrqa_gb300_series_job &J) {
+    const int64_t nc = J.n - (int64_t)(J.emb - 1) * J.tau;
+    if (!J.lam_out || nc < kLevelNc) return 0;
+    // tile levels (up to 5 planes of 128 bytes per 32x32 tile) and chunk records
+    const int64_t T = (nc + 31) / 32;
+    return (size_t)(T * (T + 1) / 2) * 5 * 128 + (size_t)T * 2 * 4096;
 }
 
 Accrqa_Error check_batch_job(const accrqa_gb300_series_job &j) { return check_job(j); }
@@ -616,12 +684,16 @@ Accrqa_Error run_batch_in(Context &c, const accrqa_gb300_series_job *jobs, int n
     Accrqa_Error err = SUCCESS;
     int j0 = 0;
     while (j0 < njobs) {
-        size_t need = 0;
+        // series data, histograms and tables add up; the tile levels and
+        // chunk records of the large series are held once per side stream
+        size_t need = 0, level = 0;
         int j1 = j0;
         while (j1 < njobs) {
             const size_t b = batch_job_bytes(jobs[j1]);
-            if (j1 > j0 && need + b > budget) break;
+            const size_t l = std::max(level, batch_job_level_bytes(jobs[j1]));
+            if (j1 > j0 && need + b + (size_t)kSideStreams * l > budget) break;
             need += b;
+            level = l;
             j1++;
         }
         if ((err = run_batch_part(c, jobs, j0, j1, rs))) return err;

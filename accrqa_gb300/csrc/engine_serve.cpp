@@ -258,7 +258,7 @@ struct accrqa_gb300_server {
                     rs.push_back(r->rs);
                 }
                 size_t need = 0;
-                for (const auto &j : jobs) need += batch_job_bytes(j);
+                for (const auto &j : jobs) need += batch_job_bytes(j) + batch_job_level_bytes(j);
                 e = run_batch_in(*c, jobs.data(), (int)jobs.size(), need + (need >> 2) + 4096,
                                  rs.data());
             }
@@ -359,7 +359,7 @@ int64_t accrqa_gb300_server_submit(Server *s, const accrqa_gb300_series_job *job
     double m = 0.0;
     if (job->dtype == ACCRQA_GB300_F64 && f64_filterable((const double *)r->job.x, job->n, &m))
         r->series_bytes += 2 * (size_t)(job->n + ACCRQA_SERIES_PAD) * 4;
-    r->bytes = batch_job_bytes(r->job) + r->series_bytes;
+    r->bytes = batch_job_bytes(r->job) + batch_job_level_bytes(r->job) + r->series_bytes;
     {
         const double nc = (double)(job->n - (int64_t)(job->emb - 1) * job->tau);
         const int measures = (job->rr_out ? 1 : 0) + (job->det_out ? 1 : 0) + (job->lam_out ? 2 : 0);

@@ -101,7 +101,7 @@ static cudaError_t launch_rp_bits_t(const void *d_x, int norm, long long nc, int
 // but not written (the caller then takes the dense rows instead).
 __global__ void compact_bins(const u64 *__restrict__ hist, long long stride, int nthr,
                              long long p, u64 *__restrict__ pairs, long long cap,
-                             unsigned long long *__restrict__ count) {
+                             unsigned long long *__restrict__ count, long long row0) {
     const int lane = threadIdx.x & 31;
     const long long gwarp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
@@ -118,7 +118,7 @@ __global__ void compact_bins(const u64 *__restrict__ hist, long long stride, int
         if (v) {
             const long long t = (long long)base + __popc(nz & ((1u << lane) - 1u));
             if (t < cap) {
-                pairs[2 * t] = ((u64)row << 40) | (u64)bin;
+                pairs[2 * t] = ((u64)(row0 + row) << 40) | (u64)bin;
                 pairs[2 * t + 1] = v;
             }
         }
@@ -129,7 +129,8 @@ __global__ void compact_bins(const u64 *__restrict__ hist, long long stride, int
 
 extern "C" int accrqa_gb300_launch_compact(const uint64_t *d_hist, int64_t stride, int32_t nthr,
                                            int64_t p, uint64_t *d_pairs, int64_t cap,
-                                           unsigned long long *d_count, void *stream) {
+                                           unsigned long long *d_count, int64_t row0,
+                                           void *stream) {
     using namespace accrqa;
     if (nthr <= 0 || p <= 0) return (int)cudaSuccess;
     if (sm_count_cached() <= 0) return (int)cudaErrorNoDevice;
@@ -138,7 +139,7 @@ extern "C" int accrqa_gb300_launch_compact(const uint64_t *d_hist, int64_t strid
     const long long cap_blocks = (long long)sm_count_cached() * 8;
     if (blocks > cap_blocks) blocks = cap_blocks;
     compact_bins<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(
-        (const u64 *)d_hist, stride, nthr, p, (u64 *)d_pairs, cap, d_count);
+        (const u64 *)d_hist, stride, nthr, p, (u64 *)d_pairs, cap, d_count, row0);
     g_launches.fetch_add(1);
     return (int)cudaGetLastError();
 }

@@ -1,9 +1,9 @@
 // noalloc.cu -- recurrence rate on device without any device allocation.
 //
-// Some callers cannot call cudaMalloc: code that runs while a CUDA stream is
-// being captured into a graph, plug-in hosts that hand a library a fixed
-// memory arena and forbid it from growing its own, and serving loops whose
-// latency budget has no room for an allocator round trip.  For them this file
+// Some callers cannot call cudaMalloc: plug-in hosts that hand a library a
+// fixed memory arena and forbid it from growing its own, and serving loops
+// whose latency budget has no room for an allocator round trip (an allocation
+// can block on the device).  For them this file
 // provides accrqa_gb300_rr_dev_noalloc: the caller passes the series and the
 // RR output in device memory, and the per-threshold 64-bit counts the RR pass
 // accumulates live in a fixed scratch array compiled into the library

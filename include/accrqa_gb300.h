@@ -359,9 +359,9 @@ Accrqa_Error accrqa_gb300_rp_bits_dev(uint32_t *d_out, const void *d_x, int32_t 
 
 /* Recurrence rate for callers that cannot allocate device memory.  No
  * counterpart in the reference: it exists for callers that may not call
- * cudaMalloc -- code running while a stream is captured into a CUDA graph,
- * hosts that give a plug-in a fixed memory arena, latency-bound serving
- * loops.  The caller passes the series d_x (device, >= n + 128 elements of
+ * cudaMalloc -- hosts that give a plug-in a fixed memory arena and forbid it
+ * from growing its own, serving loops whose latency budget has no room for an
+ * allocator round trip.  The caller passes the series d_x (device, >= n + 128 elements of
  * dtype) and the output d_rr (device, nthr values of dtype); thresholds are
  * host values of dtype.  d_rr[k] = count_k / nc^2 as the RR path computes it.
  * Work is enqueued on `stream`; the call returns without synchronising.

@@ -1,8 +1,8 @@
 """The allocation-free RR entry point against the regular device entry point.
 
 accrqa_gb300_rr_dev_noalloc is for callers that may not allocate device
-memory (code running during CUDA graph capture, hosts with a fixed memory
-arena, latency-bound serving loops): its per-threshold counts live in a
+memory (hosts with a fixed memory arena, latency-bound serving loops): its
+per-threshold counts live in a
 scratch array compiled into the library instead of memory it allocates.
 Here it is called through the C ABI twice in a row per case, and every result
 must equal what the existing entry point accrqa_gb300_rr_counts_dev gives,

@@ -734,11 +734,20 @@ def roofline_1m_section(args, peak_f32, peak_f64):
 
 def run_case(args):
     """One pass of one kernel on a smaller series (for profiler captures):
-    --case rr|det|lam, --n samples, tau=1, emb=5, 16 thresholds."""
+    --case rr|det|lam, --n samples, tau=1, emb=5, 16 thresholds.  --case batch
+    runs the batched uneven workload (--batch-series series, RR+DET+LAM)
+    warmup + steps times."""
     import torch
 
     from accrqa_gb300 import engine
     from accrqa_gb300 import workloads
+    if args.case == "batch":
+        jobs = workloads.uneven_batch(args.batch_series)
+        for _ in range(args.warmup + args.steps):
+            engine.batch(jobs)
+        torch.cuda.synchronize()
+        print(json.dumps({"case": "batch", "series": len(jobs), "done": True}))
+        return
     n = args.n
     x = workloads.lorenz_x(n, SEED).astype(np.float32)
     thr = (np.linspace(0.05, 0.8, NTHR) * float(np.std(x.astype(np.float64)))).astype(np.float32)
@@ -769,7 +778,7 @@ def run_case(args):
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--case", choices=["rr", "det", "lam"], default=None,
+    ap.add_argument("--case", choices=["rr", "det", "lam", "batch"], default=None,
                     help="run a single pass of one kernel (profiling)")
     ap.add_argument("--n", type=int, default=50_000)
     ap.add_argument("--gpus", type=int, default=1)

@@ -41,11 +41,11 @@ static cudaError_t batch_one(const accrqa_batch_launch &L, cudaStream_t st, int 
         *warps_out = sm_count_cached() * per_sm * kWarpsPerCta;
         return cudaSuccess;
     }
-    if (L.nwarps <= 0) return cudaSuccess;
+    if (L.nwarps <= 0 || L.nranges <= 0) return cudaSuccess;
     const int grid = (L.nwarps + kWarpsPerCta - 1) / kWarpsPerCta;
     kern<<<grid, kWarpsPerCta * 32, smem, st>>>((const BatchJob *)L.d_jobs,
                                                 (const BatchUnit *)L.d_units,
-                                                L.d_warp_begin, L.nwarps);
+                                                L.d_range_begin, L.nranges, L.d_queue);
     g_launches.fetch_add(1);
     return cudaGetLastError();
 }

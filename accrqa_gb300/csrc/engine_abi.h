@@ -117,6 +117,15 @@ int accrqa_gb300_launch_compact(const uint64_t *d_hist, int64_t stride, int32_t 
                                 int64_t p, uint64_t *d_pairs, int64_t cap,
                                 unsigned long long *d_count, int64_t row0, void *stream);
 
+/* Work units per resident warp of the balanced walks of this kind
+ * (accrqa_walk_kind) and embedded length: the autotuner's choice for the
+ * current device, or the default.  Passes plan their chunks with it. */
+int32_t accrqa_gb300_units_per_warp(int32_t kind, int64_t nc);
+/* Install a choice for a kind and size class (0: nc < 32768, 1: < 131072,
+ * 2: larger) on the current device. */
+void accrqa_gb300_set_units_per_warp(int32_t kind, int32_t size_class, int32_t units);
+int32_t accrqa_gb300_size_class(int64_t nc);
+
 /* Number of streaming multiprocessors of the current device (cached). */
 int accrqa_gb300_sm_count(void);
 
@@ -163,10 +172,12 @@ typedef struct accrqa_batch_launch {
     int32_t norm;
     int32_t emb;             /* the jobs' emb (they share it) */
     int32_t nt;              /* threshold slots: 8 or 16 */
-    int32_t nwarps;          /* warps in the launch (== ranges in d_warp_begin) */
+    int32_t nranges;         /* equal-cost unit ranges in d_range_begin */
+    int32_t nwarps;          /* warps the launch runs (<= resident warps) */
     const void *d_jobs;      /* accrqa_batch_job[] */
     const void *d_units;     /* accrqa_batch_unit[], ordered by job */
-    const int32_t *d_warp_begin; /* [nwarps + 1] unit range of each warp */
+    const int32_t *d_range_begin; /* [nranges + 1]: range r is units [begin[r], begin[r+1]) */
+    int32_t *d_queue;        /* the work queue: index of the next range to take, 0 at launch */
 } accrqa_batch_launch;
 
 /* Enqueue a batched launch.  Returns 0 or a cudaError_t value. */

@@ -66,6 +66,8 @@ cudaError_t side_streams(Context &c, int n) {
 namespace {
 
 constexpr int kSideStreams = 4;
+// Equal-cost unit ranges per resident warp in a batched launch's work queue.
+constexpr int kRangesPerWarp = 4;
 
 size_t align16(size_t v) { return (v + 15) & ~(size_t)15; }
 
@@ -228,7 +230,7 @@ static Accrqa_Error run_batch_part(Context &c, const accrqa_gb300_series_job *jo
     }
     struct GroupPlan {
         accrqa_batch_launch L;
-        size_t jobs_off, units_off, ranges_off;
+        size_t queue_off, jobs_off, units_off, ranges_off;
         std::vector<accrqa_batch_job> table;
         std::vector<accrqa_batch_unit> units;
         std::vector<int32_t> ranges;
@@ -299,18 +301,24 @@ static Accrqa_Error run_batch_part(Context &c, const accrqa_gb300_series_job *jo
             set_last_error("batched kernel unavailable for this shape");
             return ERR_CUDA;
         }
-        const int nw = (int)std::min<int64_t>((int64_t)resident, (int64_t)gp.units.size());
+        // kRangesPerWarp equal-cost ranges per resident warp, taken from the
+        // device work queue
+        const int nr = (int)std::min<int64_t>((int64_t)resident * kRangesPerWarp,
+                                              (int64_t)gp.units.size());
         int64_t total = 0;
         for (int64_t v : cost) total += v;
-        gp.ranges.assign((size_t)nw + 1, (int32_t)gp.units.size());
+        gp.ranges.assign((size_t)nr + 1, (int32_t)gp.units.size());
         gp.ranges[0] = 0;
         int64_t acc = 0;
         int w = 1;
-        for (size_t u = 0; u < gp.units.size() && w < nw; u++) {
+        for (size_t u = 0; u < gp.units.size() && w < nr; u++) {
             acc += cost[u];
-            while (w < nw && acc * nw >= total * w) gp.ranges[(size_t)w++] = (int32_t)(u + 1);
+            while (w < nr && acc * nr >= total * w) gp.ranges[(size_t)w++] = (int32_t)(u + 1);
         }
-        gp.L.nwarps = nw;
+        gp.L.nranges = nr;
+        gp.L.nwarps = std::min(resident, nr);
+        gp.queue_off = align16(off);
+        off = gp.queue_off + 16;
         gp.jobs_off = align16(off);
         off = gp.jobs_off + gp.table.size() * sizeof(accrqa_batch_job);
         gp.units_off = align16(off);
@@ -433,7 +441,9 @@ static Accrqa_Error run_batch_part(Context &c, const accrqa_gb300_series_job *jo
         std::memcpy(host + gp.ranges_off, gp.ranges.data(), gp.ranges.size() * sizeof(int32_t));
         gp.L.d_jobs = dev + gp.jobs_off;
         gp.L.d_units = dev + gp.units_off;
-        gp.L.d_warp_begin = (const int32_t *)(dev + gp.ranges_off);
+        gp.L.d_range_begin = (const int32_t *)(dev + gp.ranges_off);
+        std::memset(host + gp.queue_off, 0, 16);   // the queue starts at range 0
+        gp.L.d_queue = (int32_t *)(dev + gp.queue_off);
     }
     // series and tables in two copies (the result region between them is zeroed)
     if (series_bytes)

@@ -157,11 +157,53 @@ extern "C" int accrqa_gb300_launch_rp_bits(const void *d_x, int32_t dtype, int32
     return (int)cudaErrorInvalidValue;
 }
 
+// Units per resident warp of the balanced walks, per device, walk kind and
+// size class: the hand-measured defaults until accrqa_gb300_autotune
+// installs its measured choice.
+static std::atomic<int> g_units_per_warp[64][3][3];
+static std::atomic<bool> g_units_init[64];
+
+static std::atomic<int> *units_slot(int kind, int cls) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+        cudaGetLastError();
+        dev = 0;
+    }
+    if (!g_units_init[dev].load()) {
+        static std::mutex mu;
+        std::lock_guard<std::mutex> g(mu);
+        if (!g_units_init[dev].load()) {
+            for (int c = 0; c < 3; c++) {
+                g_units_per_warp[dev][ACCRQA_WALK_RR][c].store(8);
+                g_units_per_warp[dev][ACCRQA_WALK_DET][c].store(accrqa::kDetUnitsPerWarp);
+                g_units_per_warp[dev][ACCRQA_WALK_LAM][c].store(accrqa::kLamUnitsPerWarp);
+            }
+            g_units_init[dev].store(true);
+        }
+    }
+    return &g_units_per_warp[dev][kind][cls];
+}
+
+extern "C" int32_t accrqa_gb300_size_class(int64_t nc) {
+    return nc < 32768 ? 0 : nc < 131072 ? 1 : 2;
+}
+
+extern "C" int32_t accrqa_gb300_units_per_warp(int32_t kind, int64_t nc) {
+    if (kind < 0 || kind > 2) return 16;
+    return units_slot(kind, accrqa_gb300_size_class(nc))->load();
+}
+
+extern "C" void accrqa_gb300_set_units_per_warp(int32_t kind, int32_t cls, int32_t units) {
+    if (kind < 0 || kind > 2 || cls < 0 || cls > 2 || units < 1) return;
+    units_slot(kind, cls)->store(units);
+}
+
 extern "C" int64_t accrqa_gb300_walk_scratch_bytes(const accrqa_walk_desc *d) {
     using namespace accrqa;
     if (!d || d->nc < 2 || (d->kind != ACCRQA_WALK_DET && d->kind != ACCRQA_WALK_LAM)) return 0;
     const int nt = d->nthr <= 4 ? 4 : d->nthr <= 8 ? 8 : 16;   // slots of the instantiation
-    const LinePlan q = plan_lines(d->kind == ACCRQA_WALK_DET, d->nc, sm_count_cached(), true);
+    const LinePlan q = plan_lines(d->kind == ACCRQA_WALK_DET, d->nc, sm_count_cached(), true,
+                                  accrqa_gb300_units_per_warp(d->kind, d->nc));
     return (int64_t)q.nrecords * nt * 32 * 2 * (int64_t)sizeof(u32);
 }
 

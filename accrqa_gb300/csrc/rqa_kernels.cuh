@@ -52,9 +52,10 @@ template <typename T> constexpr int row_min_ctas() {
 template <typename T, int EMB> constexpr int rr_min_ctas() {
     return !std::is_same<T, F64F>::value && EMB > 0 && EMB <= 3 ? 5 : kWideMinCtas;
 }
-// Work units per resident warp the chunked line walks aim at (0: the walk
-// never chunks).  Chunking DET evens out its unequal diagonals; LAM rows are
-// equal, and its grid only chunks when it would leave warps idle.
+// Work units per resident warp the chunked line walks aim at by default
+// (accrqa_gb300_autotune measures and replaces them per walk kind and size
+// class).  Chunking DET evens out its unequal diagonals; LAM rows are equal,
+// and its grid only chunks when it would leave warps idle.
 constexpr int kDetUnitsPerWarp = 16;
 constexpr int kLamUnitsPerWarp = 16;
 constexpr int kSeriesPad = 128;
@@ -711,17 +712,16 @@ struct LinePlan {
     long long nrecords;  // boundary records (0 = whole lines, no stitch)
 };
 
-// Chunks are sized for k{Det,Lam}UnitsPerWarp units per resident warp (at
-// most 8 CTAs of kWarpsPerCta warps per SM); a chunk spans at least 8
-// blocks, and a walk whose bands alone reach the target goes whole.  Whole
-// DET lines pair band b with band nbands-1-b (every pair walks about nc
-// cells per lane).
-inline LinePlan plan_lines(bool det, long long nc, int sms, bool allow_chunks) {
+// Chunks are sized for `units_per_warp` units per resident warp (at most 8
+// CTAs of kWarpsPerCta warps per SM); a chunk spans at least 8 blocks, and a
+// walk whose bands alone reach the target goes whole.  Whole DET lines pair
+// band b with band nbands-1-b (every pair walks about nc cells per lane).
+inline LinePlan plan_lines(bool det, long long nc, int sms, bool allow_chunks,
+                           int units_per_warp) {
     LinePlan q;
     q.nbands = det ? (nc - 1 + 31) / 32 : (nc + 31) / 32;
     const long long blocks = det ? q.nbands * (q.nbands + 1) / 2 : q.nbands * q.nbands;
-    const long long target = (long long)(det ? kDetUnitsPerWarp : kLamUnitsPerWarp) * sms * 8 *
-                             kWarpsPerCta;
+    const long long target = (long long)units_per_warp * sms * 8 * kWarpsPerCta;
     long long B = target > 0 ? (blocks + target - 1) / target : q.nbands;
     if (B < 8) B = 8;
     long long K = q.nbands > 0 ? (q.nbands + B - 1) / B : 1;

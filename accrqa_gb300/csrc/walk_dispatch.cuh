@@ -93,12 +93,12 @@ static cudaError_t per_sm_of(K kern, size_t smem, std::atomic<int> &cache, int *
 }
 
 // (band, chunk) units of equal size over the upper-triangle tiles of
-// `bands` 32-row bands, about 8 per resident warp or more (the RR walk and
-// the level walk's first phase).
+// `bands` 32-row bands, about `per_warp` per resident warp or more (the RR
+// walk and the level walk's first phase).
 static void plan_upper_units(long long bands, long long resident, long long *chunk,
-                             long long *nunits) {
+                             long long *nunits, int per_warp) {
     const long long total_blocks = bands * (bands + 1) / 2;
-    long long B = total_blocks / (8 * resident);
+    long long B = total_blocks / ((long long)per_warp * resident);
     B = B < 8 ? 8 : (B > 256 ? 256 : B);
     *chunk = B;
     *nunits = bands * ((bands + B - 1) / B);
@@ -151,17 +151,18 @@ static cudaError_t launch_levels_one(const accrqa_walk_desc &d, cudaStream_t st)
 
     if (!d.planes_ready) {
         plan_upper_units(T_, (long long)sm_count_cached() * per1 * kWarpsPerCta, &a.chunk,
-                         &a.nunits);
+                         &a.nunits, accrqa_gb300_units_per_warp(ACCRQA_WALK_RR, d.nc));
         tile_levels<T, NORM, EMB, NT><<<grid_for(a.nunits, per1), kWarpsPerCta * 32, 0, st>>>(a);
         g_launches.fetch_add(1);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
 
     // chunked when the caller's scratch holds the boundary records
-    LinePlan q = plan_lines(det, d.nc, sm_count_cached(), d.d_scratch != nullptr);
+    const int upw = accrqa_gb300_units_per_warp(d.kind, d.nc);
+    LinePlan q = plan_lines(det, d.nc, sm_count_cached(), d.d_scratch != nullptr, upw);
     const long long rec = q.nrecords * NT * 32 * 2 * (long long)sizeof(u32);
     if (q.nrecords > 0 && rec > d.scratch_bytes)
-        q = plan_lines(det, d.nc, sm_count_cached(), false);
+        q = plan_lines(det, d.nc, sm_count_cached(), false, upw);
     a.nbands = q.nbands;
     a.nunits = q.nunits;
     a.chunk = q.chunk;
@@ -202,10 +203,11 @@ static cudaError_t launch_one(const accrqa_walk_desc &d, cudaStream_t st) {
     if (KIND != ACCRQA_WALK_RR) {
         // chunked when the caller's scratch holds the boundary records
         const bool det = KIND == ACCRQA_WALK_DET;
-        q = plan_lines(det, d.nc, sm_count_cached(), d.d_scratch != nullptr);
+        const int upw = accrqa_gb300_units_per_warp(KIND, d.nc);
+        q = plan_lines(det, d.nc, sm_count_cached(), d.d_scratch != nullptr, upw);
         const long long need = q.nrecords * NT * 32 * 2 * (long long)sizeof(u32);
         if (q.nrecords > 0 && need > d.scratch_bytes)
-            q = plan_lines(det, d.nc, sm_count_cached(), false);
+            q = plan_lines(det, d.nc, sm_count_cached(), false, upw);
         a.nbands = q.nbands;
         a.nunits = q.nunits;
         a.chunk = q.chunk;
@@ -216,7 +218,7 @@ static cudaError_t launch_one(const accrqa_walk_desc &d, cudaStream_t st) {
     } else {
         a.nbands = (d.nc + 31) / 32;
         plan_upper_units(a.nbands, (long long)sm_count_cached() * per_sm * kWarpsPerCta,
-                         &a.chunk, &a.nunits);
+                         &a.chunk, &a.nunits, accrqa_gb300_units_per_warp(ACCRQA_WALK_RR, d.nc));
     }
     if (a.nunits <= 0) return cudaSuccess;
     kern<<<grid_for(a.nunits, per_sm), kWarpsPerCta * 32, smem, st>>>(a);

@@ -198,6 +198,19 @@ def batch(jobs, measures=("rr", "det", "lam")):
     return outs
 
 
+def autotune() -> str:
+    """Time the balanced walks' chunk granularity on this GPU and install the
+    fastest per walk kind and length class (accrqa_gb300_autotune); returns
+    the choices."""
+    lib = _lib.handle()
+    f = lib.accrqa_gb300_autotune
+    f.argtypes = [ctypes.c_char_p, ctypes.c_int64]
+    f.restype = ctypes.c_int
+    buf = ctypes.create_string_buffer(1024)
+    _check(f(buf, len(buf)), "autotune")
+    return buf.value.decode()
+
+
 class Server:
     """Continuous-batching request server (accrqa_gb300_server_*).
 

@@ -231,6 +231,10 @@ def run_ours(args):
                     s1.record(stream)
                     ev[kind].append((s0, s1, nc, e))
 
+    # the chunk granularity of the balanced walks, measured on this GPU
+    # (about a second, before the warm-up and outside every timed region)
+    tuned = engine.autotune()
+    log(f"autotune: {tuned}")
     log("inputs ready; warm-up")
     for _ in range(args.warmup):
         step(False)
@@ -325,6 +329,7 @@ def run_ours(args):
                 "d2h_bytes_per_step": int(d2h.value // e2e_steps),
                 "path": "accrqa_gb300.RR/DET/LAM -> py_accrqa_* (host numpy buffers)"},
         "gpu_launches": int(launches),
+        "autotune": tuned,
         "roofline": {"bound": "fp32", "kernel": dom,
                      "pass_kernels": {"rr": "rr_rows", "det": "det_diags + line_stitch",
                                       "lam": "tile_levels + lam_levels + line_stitch"}[dom],

@@ -194,6 +194,15 @@ void accrqa_gb300_transfer_stats(uint64_t *h2d_bytes, uint64_t *d2h_bytes,
 /* Number of CUDA kernels the engine has launched since load. */
 uint64_t accrqa_gb300_kernel_launches(void);
 
+/* Autotuner (no counterpart in the reference): times the balanced walks' chunk
+ * granularity -- work units per resident warp, RR {4, 8, 16}, DET and LAM
+ * {8, 16, 32} -- on the current device for three series-length classes and
+ * installs the fastest for the calls that follow (process-wide, per device;
+ * call it before other work, it takes about a second).  Results never depend
+ * on the choice, only the time.  The choices and their times are written to
+ * report (report_bytes, may be null). */
+Accrqa_Error accrqa_gb300_autotune(char *report, int64_t report_bytes);
+
 /* Testing hook: the next `count` device allocations the engine makes fail on
  * the host with an out-of-memory error before reaching the driver (0
  * cancels), so that callers can see how failures surface: the public calls

@@ -33,10 +33,12 @@ def line_record(det, nbands, chunk, c, b):
     return c * nbands - chunk * (c * (c - 1) // 2) + b if det else c * nbands + b
 
 
-def plan_lines(det, nc, sms, allow=True):
+def plan_lines(det, nc, sms, allow=True, units=None):
     nbands = (nc - 1 + 31) // 32 if det else (nc + 31) // 32
     blocks = nbands * (nbands + 1) // 2 if det else nbands * nbands
-    target = (DET_UNITS_PER_WARP if det else LAM_UNITS_PER_WARP) * sms * 8 * WARPS_PER_CTA
+    if units is None:   # the defaults until the autotuner replaces them
+        units = DET_UNITS_PER_WARP if det else LAM_UNITS_PER_WARP
+    target = units * sms * 8 * WARPS_PER_CTA
     B = -(-blocks // target) if target > 0 else nbands
     B = max(B, 8)
     K = -(-nbands // B) if nbands > 0 else 1
@@ -51,13 +53,14 @@ def plan_lines(det, nc, sms, allow=True):
 
 @pytest.mark.parametrize("det", [True, False])
 @pytest.mark.parametrize("sms", [1, 8, 152])
-def test_plan_covers_blocks_and_records_once(det, sms):
+@pytest.mark.parametrize("units", [None, 4, 8, 32])   # the autotuner's candidates
+def test_plan_covers_blocks_and_records_once(det, sms, units):
     rng = np.random.default_rng(5)
     sizes = [2, 3, 31, 32, 33, 64, 65, 257, 1000, 4097, 20000, 200000, 199944]
     sizes += [int(v) for v in rng.integers(2, 60000, 20)]
     chunked = 0
     for nc in sizes:
-        q = plan_lines(det, nc, sms)
+        q = plan_lines(det, nc, sms, units=units)
         nb, B = q["nbands"], q["chunk"]
         if q["nrecords"] == 0:
             continue

@@ -9,6 +9,7 @@
 #include <cstring>
 
 #include "engine_abi.h"
+#include "rqa_diag.cuh"
 #include "rqa_kernels.cuh"
 #include "rqa_planes.cuh"
 
@@ -178,9 +179,70 @@ static cudaError_t launch_levels_one(const accrqa_walk_desc &d, cudaStream_t st)
     return launch_stitch<NT>(a, det, st);
 }
 
+// Which RR walk a float pass takes.  The diagonal walk evaluates one
+// distance term per cell instead of emb, but its warp-wide skip groups are
+// less often empty than the row walk's 32 x 8 cell patches, so the threshold
+// work it saves on distances is partly spent again on compares.  Measured on
+// the GB300 (Lorenz x, N = 200,000, 16 thresholds, ms per pass, diagonal /
+// rows): tau 1: emb 3 22.4 / 17.6, emb 5 22.8 / 20.3, emb 8 20.4 / 24.6;
+// tau 2: 19.8 / 17.3, 19.2 / 19.4, 16.0 / 23.4; tau 4: 17.4 / 16.3,
+// 15.3 / 18.1, 13.1 / 22.5; tau 8: 15.6 / 14.9, 13.6 / 17.1, 12.1 / 21.7;
+// and with 4 thresholds (N = 1e6, tau 1, emb 5) 0.27 / 0.33 s.  The diagonal
+// walk wins once the term window spans (emb - 1) tau >= 7 positions with
+// emb >= 4, or with few thresholds, where the distance is most of the work.
+// Its 32-bit series indices need n + ACCRQA_SERIES_PAD < 2^31.
+inline bool rr_along_diagonals(int emb, int tau, int nthr, long long nc) {
+    if (nc + (long long)(emb - 1) * tau + ACCRQA_SERIES_PAD >= (1LL << 31)) return false;
+    return emb >= 4 && ((long long)(emb - 1) * tau >= 7 || nthr <= 4);
+}
+
+// RR of a float series with a fixed embedding, along diagonals
+// (rqa_diag.cuh): the main diagonal, then the strict upper triangle in
+// (band of diagonals, chunk of positions) units, about `per_warp` per
+// resident warp.
+template <int NORM, int EMB, int NT>
+static cudaError_t launch_rr_diag(const accrqa_walk_desc &d, cudaStream_t st) {
+    static std::atomic<int> c_diag{-1};
+    int per_sm = 0;
+    cudaError_t e = per_sm_of(rr_diags<NORM, EMB, NT>, 0, c_diag, &per_sm);
+    if (e != cudaSuccess) return e;
+    WalkArgs a;
+    fill_walk_args<float>(d, a);
+    const long long sms = sm_count_cached();
+    long long g0 = (d.nc + 255) / 256;
+    if (g0 > sms * 4) g0 = sms * 4;
+    if (g0 > 0) {
+        rr_main_diag<NORM, EMB, NT><<<(unsigned)g0, 256, 0, st>>>(a);
+        g_launches.fetch_add(1);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    if (d.nc < 2) return cudaSuccess;
+    // bands of 2A diagonals, A = 32 / min(tau, 32) (the kernel's lane map)
+    const long long W = 2 * (32 / (d.tau < 32 ? d.tau : 32));
+    a.nbands = (d.nc - 1 + W - 1) / W;
+    // cells of the strict upper triangle over W-diagonal x C-position units
+    const long long resident = sms * per_sm * kWarpsPerCta;
+    const long long target = (long long)accrqa_gb300_units_per_warp(ACCRQA_WALK_RR, d.nc) * resident;
+    const long long cells = d.nc * (d.nc - 1) / 2;
+    long long C = (cells + W * target - 1) / (W * target);
+    // at least four groups per residue class, at most a few KB of series
+    // per lane window so that a chunk's residue walks share L1
+    const long long cmin = 4LL * rr_diag_group<EMB>() * d.tau;
+    if (C > 4096) C = 4096;
+    if (C < cmin) C = cmin;
+    if (C < 64) C = 64;
+    a.chunk = C;
+    a.nunits = a.nbands * ((d.nc - 1 + C - 1) / C);
+    rr_diags<NORM, EMB, NT><<<grid_for(a.nunits, per_sm), kWarpsPerCta * 32, 0, st>>>(a);
+    g_launches.fetch_add(1);
+    return cudaGetLastError();
+}
+
 template <int KIND, typename T, int NORM, int EMB, int NT>
 static cudaError_t launch_one(const accrqa_walk_desc &d, cudaStream_t st) {
     if constexpr (KIND == kWalkLevels) return launch_levels_one<T, NORM, EMB, NT>(d, st);
+    if constexpr (KIND == ACCRQA_WALK_RR && std::is_same<T, float>::value && EMB > 0)
+        if (rr_along_diagonals(EMB, d.tau, d.nthr, d.nc)) return launch_rr_diag<NORM, EMB, NT>(d, st);
     void (*kern)(WalkArgs);
     size_t smem = 0;
     // if constexpr: a translation unit instantiates only its own kind

@@ -43,6 +43,36 @@ def test_counts_and_histograms_match_oracle(gpu, oracle_mod, dt, norm, n, tau, e
         np.testing.assert_array_equal(lam[k], oracle_mod.lam_hist(x, tau, emb, t, norm))
 
 
+def _diag_cases():
+    # float series with a fixed embedding whose RR takes the diagonal walk
+    # (emb >= 4 and (emb - 1) tau >= 7, or at most 4 thresholds): residue
+    # blocks for tau dividing 32 or not, tau above 32, lengths around the
+    # band and chunk edges
+    rng = np.random.default_rng(23)
+    out = []
+    for norm in NORMS:
+        for (n, tau, emb) in [(50, 1, 4), (66, 1, 4), (200, 2, 4), (1000, 3, 4), (777, 5, 6),
+                              (900, 7, 4), (2100, 33, 4), (3000, 40, 5), (400, 16, 8),
+                              (1300, 32, 4), (129, 2, 8), (4000, 1, 8), (2500, 8, 5)]:
+            out.append((norm, n, tau, emb, int(rng.integers(0, 1 << 30))))
+    return out
+
+
+@pytest.mark.parametrize("norm,n,tau,emb,seed", _diag_cases())
+def test_rr_diagonal_walk_matches_oracle(gpu, oracle_mod, norm, n, tau, emb, seed):
+    x = workloads.logistic(n, seed).astype(np.float32)
+    if seed % 2 == 0:
+        x = (np.round(x * 16) / 16).astype(np.float32)   # exact ties at the thresholds
+    if seed % 5 == 0:
+        x[n // 3] = np.nan                                # NaN and inf cells, main diagonal too
+        x[n // 2] = np.inf
+    few = np.array([0.05, 0.125, 0.25, 0.5], np.float32)
+    many = np.linspace(0.0, 1.0, 12).astype(np.float32)
+    for thr in (few, many):
+        np.testing.assert_array_equal(gpu.rr_counts(x, tau, emb, thr, norm),
+                                      oracle_mod.rr_counts(x, tau, emb, thr, norm))
+
+
 @pytest.mark.parametrize("nthr", [1, 3, 4, 5, 8, 9, 16, 17, 40])
 def test_threshold_pass_splitting(gpu, oracle_mod, nthr):
     x = workloads.white(400, 5 + nthr).astype(np.float32)

@@ -80,6 +80,13 @@ struct WalkArgs {
     // the upper-triangle tiles and the number of 32-row tile bands.
     u32 *planes;
     long long tbands;
+    // RR of float series with more than 8 thresholds: the cells are counted
+    // by level from a bucket table (rqa_level_table.cuh) when lt_on is set:
+    // buckets bits >> lt_shift, lt_nb of them from lt_lo
+    int lt_on;
+    int lt_shift;
+    u32 lt_lo;
+    int lt_nb;
 };
 
 // ---------------------------------------------------------------------------

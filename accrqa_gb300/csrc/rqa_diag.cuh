@@ -28,6 +28,7 @@
 #pragma once
 
 #include "rqa_kernels.cuh"
+#include "rqa_level_table.cuh"
 
 namespace accrqa {
 
@@ -142,6 +143,26 @@ __device__ __forceinline__ bool diag_rr_push(u32 (&m)[NT], const f2 (&v)[GS],
 
 // Mask bits into the lane's counters, which live in shared memory (slot k
 // at cnt[32 k]): registers hold the term window, the group and the masks.
+// Levels variant of the push (more than 8 thresholds): the cells of a
+// non-skipped group are counted by level into the lane's histogram.
+// A lane with `on` false (no cells of its own) counts nothing.
+template <int GS>
+__device__ __forceinline__ void diag_rr_levels(const f2 (&v)[GS],
+                                               const u64 (&keys)[kMaxThrPerPass],
+                                               const uint4 *tbl, int shift, int base, int nb,
+                                               u32 *h, bool on) {
+    u64 any = 0;
+#pragma unroll
+    for (int j = 0; j < GS; j++) any |= sub2(v[j], keys[0]);
+    if (!__any_sync(0xFFFFFFFFu, ((u32)any | (u32)(any >> 32)) >> 31)) return;
+    if (!on) return;
+#pragma unroll
+    for (int j = 0; j < GS; j++) {
+        level_count(h, level_of(lo_of(v[j]), tbl, shift, base, nb));
+        level_count(h, level_of(hi_of(v[j]), tbl, shift, base, nb));
+    }
+}
+
 template <int NT>
 __device__ __forceinline__ void diag_rr_flush(u32 (&m)[NT], u32 *cnt, bool on) {
 #pragma unroll
@@ -184,14 +205,26 @@ rr_main_diag(const __grid_constant__ WalkArgs p) {
 // stretched along the diagonals is far more often empty than one across
 // them).  p.nbands bands of 2A diagonals, chunks of p.chunk positions,
 // p.nunits units chunk-major.
-template <int NORM, int EMB, int NT>
+// LEVELS (16 slots): the cells are counted by level from the pass's bucket
+// table (rqa_level_table.cuh) instead of by slot masks.
+template <int NORM, int EMB, int NT, bool LEVELS = false>
 __global__ void __launch_bounds__(kWarpsPerCta * 32, kRrDiagMinCtas)
 rr_diags(const __grid_constant__ WalkArgs p) {
     constexpr int GS = rr_diag_group<EMB>();
-    __shared__ u32 cnt_cta[kWarpsPerCta * NT * 32];
+    // masks: per-lane slot counters; levels: the table and per-lane level
+    // histograms (slot counts of a lane are flushed per unit either way)
+    constexpr int kCnt = LEVELS ? (NT + 1) * 32 : NT * 32;
+    __shared__ u32 cnt_cta[kWarpsPerCta * kCnt];
+    __shared__ uint4 tbl[LEVELS ? kLevelTableMax + 2 : 1];
+    if constexpr (LEVELS) {
+        level_table_build(tbl, p);
+        for (int t = threadIdx.x; t < kWarpsPerCta * kCnt; t += blockDim.x) cnt_cta[t] = 0;
+        __syncthreads();
+    }
+    const int shift = p.lt_shift, base = (int)p.lt_lo - 1, nb = p.lt_nb;
     const float *x = (const float *)p.x;
     const int lane = threadIdx.x & 31;
-    u32 *cnt = cnt_cta + (threadIdx.x >> 5) * NT * 32 + lane;
+    u32 *cnt = cnt_cta + (threadIdx.x >> 5) * kCnt + lane;
     const long long gwarp = (long long)blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);
     const long long nwarps = (long long)gridDim.x * kWarpsPerCta;
     const long long nc = p.nc;
@@ -216,8 +249,10 @@ rr_diags(const __grid_constant__ WalkArgs p) {
         // positions below `safe` are cells of both diagonals of every lane
         const long long safe_all = nc - (d0 + 2 * A - 1);
         const long long safe = se < safe_all ? se : safe_all;
+        if constexpr (!LEVELS) {
 #pragma unroll
-        for (int k = 0; k < NT; k++) cnt[32 * k] = 0;
+            for (int k = 0; k < NT; k++) cnt[32 * k] = 0;
+        }
         for (int rb = 0; rb < tau; rb += R) {
             const long long s_min = sb + rb;     // the block's first residue
             if (s_min >= se) break;              // warp-uniform
@@ -239,7 +274,9 @@ rr_diags(const __grid_constant__ WalkArgs p) {
             for (; sm + span + (GS - 1) * tau < safe; s += GS * tau, sm += GS * tau) {
                 f2 v[GS];
                 diag_rr_group<NORM, EMB, GS, false>(v, w, x, (int)dA, A, s, sm, tau, se, lenA);
-                if (diag_rr_push<NT, GS>(msk, v, p.keys)) {
+                if constexpr (LEVELS)
+                    diag_rr_levels<GS>(v, p.keys, tbl, shift, base, nb, cnt, on);
+                else if (diag_rr_push<NT, GS>(msk, v, p.keys)) {
                     nbits += 2 * GS;
                     if (nbits + 2 * GS > 32) {
                         diag_rr_flush<NT>(msk, cnt, on);
@@ -250,7 +287,9 @@ rr_diags(const __grid_constant__ WalkArgs p) {
             for (; sm < se; s += GS * tau, sm += GS * tau) {
                 f2 v[GS];
                 diag_rr_group<NORM, EMB, GS, true>(v, w, x, (int)dA, A, s, sm, tau, se, lenA);
-                if (diag_rr_push<NT, GS>(msk, v, p.keys)) {
+                if constexpr (LEVELS)
+                    diag_rr_levels<GS>(v, p.keys, tbl, shift, base, nb, cnt, on);
+                else if (diag_rr_push<NT, GS>(msk, v, p.keys)) {
                     nbits += 2 * GS;
                     if (nbits + 2 * GS > 32) {
                         diag_rr_flush<NT>(msk, cnt, on);
@@ -258,14 +297,18 @@ rr_diags(const __grid_constant__ WalkArgs p) {
                     }
                 }
             }
-            diag_rr_flush<NT>(msk, cnt, on);
+            if constexpr (!LEVELS) diag_rr_flush<NT>(msk, cnt, on);
         }
+        if constexpr (LEVELS) {
+            level_flush<NT>(cnt, total, 2u);   // (i, j) and (j, i)
+        } else {
 #pragma unroll
-        for (int k = 0; k < NT; k++) {
-            u32 t = cnt[32 * k];
+            for (int k = 0; k < NT; k++) {
+                u32 t = cnt[32 * k];
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xFFFFFFFFu, t, o);
-            if (lane == k) total += 2ull * (u64)t;   // (i, j) and (j, i)
+                for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xFFFFFFFFu, t, o);
+                if (lane == k) total += 2ull * (u64)t;   // (i, j) and (j, i)
+            }
         }
     }
     if (lane < p.nthr && lane < NT && total) atomicAdd(&p.counts[p.row[lane]], total);

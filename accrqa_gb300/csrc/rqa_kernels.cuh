@@ -31,6 +31,7 @@
 #pragma once
 
 #include "rqa_device.cuh"
+#include "rqa_level_table.cuh"
 
 namespace accrqa {
 
@@ -829,6 +830,97 @@ rr_rows(const __grid_constant__ WalkArgs p) {
         }
     }
     if (lane < p.nthr && lane < NT && total) atomicAdd(&p.counts[p.row[lane]], total);
+}
+
+// ---------------------------------------------------------------------------
+// RR by levels (float, fixed embedding, more than 8 thresholds): rr_rows'
+// walk, each non-skipped group's cells counted by level (rqa_level_table.cuh)
+// into per-lane histograms instead of pushed into 16 slot masks.
+// ---------------------------------------------------------------------------
+template <int NORM, int EMB, bool CHECK>
+__device__ __forceinline__ void rr_block_levels(const LaneVec<float, EMB> &a,
+                                                const float *__restrict__ xj, long long tau,
+                                                long long lo, long long hi,
+                                                const u64 (&keys)[kMaxThrPerPass], float *stage,
+                                                const uint4 *tbl, int shift, int base, int nb,
+                                                u32 *h) {
+    __syncwarp();   // the previous block's reads are done
+    RowStage<float, EMB>::load(stage, xj, tau);
+    __syncwarp();
+#pragma unroll 1
+    for (int g = 0; g < 32; g += kGroup) {
+        f2 v[kGroup / 2];
+        row_group_staged<NORM, EMB, CHECK>(v, a, stage, g, lo, hi);
+        u64 any = 0;
+#pragma unroll
+        for (int q = 0; q < kGroup / 2; q++) any |= sub2(v[q], keys[0]);
+        if (!__any_sync(0xFFFFFFFFu, ((u32)any | (u32)(any >> 32)) >> 31)) continue;
+#pragma unroll
+        for (int q = 0; q < kGroup / 2; q++) {
+            level_count(h, level_of(lo_of(v[q]), tbl, shift, base, nb));
+            level_count(h, level_of(hi_of(v[q]), tbl, shift, base, nb));
+        }
+    }
+}
+
+template <int NORM, int EMB>
+__global__ void __launch_bounds__(kWarpsPerCta * 32, rr_min_ctas<float, EMB>())
+rr_rows_levels(const __grid_constant__ WalkArgs p) {
+    constexpr int NT = kMaxThrPerPass;
+    __shared__ __align__(16) float stage_cta[kWarpsPerCta * RowStage<float, EMB>::kWords];
+    __shared__ uint4 tbl[kLevelTableMax + 2];
+    __shared__ u32 hist_cta[kWarpsPerCta * (NT + 1) * 32];
+    level_table_build(tbl, p);
+    for (int t = threadIdx.x; t < kWarpsPerCta * (NT + 1) * 32; t += blockDim.x) hist_cta[t] = 0;
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float *stage = stage_cta + warp * RowStage<float, EMB>::kWords;
+    u32 *h = hist_cta + warp * (NT + 1) * 32 + lane;
+    const float *x = (const float *)p.x;
+    const long long gwarp = (long long)blockIdx.x * kWarpsPerCta + warp;
+    const long long nwarps = (long long)gridDim.x * kWarpsPerCta;
+    const long long nc = p.nc, tau = p.tau;
+    const int shift = p.lt_shift, base = (int)p.lt_lo - 1, nb = p.lt_nb;
+    u64 total = 0;
+    const long long nbands = p.nbands, B = p.chunk;
+
+    for (long long unit = gwarp; unit < p.nunits; unit += nwarps) {
+        const long long band = unit % nbands, chunk = unit / nbands;
+        const long long j0 = band * 32;
+        const long long nblk = (nc - j0 + 31) / 32;
+        long long kb = chunk * B;
+        if (kb >= nblk) continue;                     // warp-uniform
+        const long long ke = kb + B < nblk ? kb + B : nblk;
+        const long long i = j0 + lane;
+        const bool row_ok = i < nc;
+        LaneVec<float, EMB> a;
+        a.load(x + i, tau);
+        u32 dlev = 0;   // level of the lane's main-diagonal cell (counted once)
+        if (kb == 0) {
+            const float v = cell_dist_mem<float, NORM, EMB>(x + i, x + i, tau, p.emb);
+            dlev = row_ok ? level_of(v, tbl, shift, base, nb) : 0u;
+            const long long hi0 = nc - j0 < 32 ? nc - j0 : 32;
+            rr_block_levels<NORM, EMB, true>(a, x + j0, tau, lane + 1, hi0, p.keys, stage, tbl,
+                                             shift, base, nb, h);
+            kb = 1;
+        }
+        const long long kfull = (nc - j0) / 32 < ke ? (nc - j0) / 32 : ke;
+        long long k = kb;
+        for (; k < kfull; k++)
+            rr_block_levels<NORM, EMB, false>(a, x + j0 + 32 * k, tau, 0, 32, p.keys, stage, tbl,
+                                              shift, base, nb, h);
+        if (k < ke)
+            rr_block_levels<NORM, EMB, true>(a, x + j0 + 32 * k, tau, 0, nc - j0 - 32 * k, p.keys,
+                                             stage, tbl, shift, base, nb, h);
+        // the cells of rows past nc are discarded
+        level_flush<NT>(h, total, 2u, row_ok);
+#pragma unroll
+        for (int s = 0; s < NT; s++) {
+            const u32 c = (u32)__popc(__ballot_sync(0xFFFFFFFFu, dlev > (u32)s));
+            if (lane == s) total += c;
+        }
+    }
+    if (lane < p.nthr && total) atomicAdd(&p.counts[p.row[lane]], total);
 }
 
 // ---------------------------------------------------------------------------

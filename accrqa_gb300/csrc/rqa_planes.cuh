@@ -185,6 +185,193 @@ tile_levels(const __grid_constant__ WalkArgs p) {
 }
 
 // ---------------------------------------------------------------------------
+// tile_levels by levels (float, fixed embedding, 16 slots, the pass's limits
+// admit a bucket table): the same tiles, units and stores as tile_levels, but
+// each non-skipped group's cells are given their level from the table
+// (rqa_level_table.cuh) and pushed straight into the planes, instead of
+// deciding 16 slot masks and folding them into planes.
+// ---------------------------------------------------------------------------
+template <int NORM, int EMB, bool CHECK>
+__device__ __forceinline__ void row_planes_levels(u32 (&P)[Planes<16>::kN],
+                                                  const LaneVec<float, EMB> &a,
+                                                  const float *__restrict__ xj, long long tau,
+                                                  long long lo, long long hi,
+                                                  const u64 (&keys)[kMaxThrPerPass], float *stage,
+                                                  const uint4 *tbl, int shift, int base, int nb) {
+    constexpr int NP = Planes<16>::kN;
+    __syncwarp();   // the previous block's reads are done
+    RowStage<float, EMB>::load(stage, xj, tau);
+    __syncwarp();
+#pragma unroll 1
+    for (int g = 0; g < 32; g += kGroup) {
+        f2 v[kGroup / 2];
+        row_group_staged<NORM, EMB, CHECK>(v, a, stage, g, lo, hi);
+        u64 any = 0;
+#pragma unroll
+        for (int q = 0; q < kGroup / 2; q++) any |= sub2(v[q], keys[0]);
+        if (!__any_sync(0xFFFFFFFFu, ((u32)any | (u32)(any >> 32)) >> 31)) {
+#pragma unroll
+            for (int b = 0; b < NP; b++) P[b] <<= kGroup;   // level 0 everywhere
+            continue;
+        }
+        levels_push8<NP>(P, v, tbl, shift, base, nb);
+    }
+}
+
+template <int NORM, int EMB>
+__global__ void __launch_bounds__(kWarpsPerCta * 32, rr_min_ctas<float, EMB>())
+tile_levels_lt(const __grid_constant__ WalkArgs p) {
+    constexpr int NP = Planes<16>::kN;
+    __shared__ __align__(16) float stage_cta[kWarpsPerCta * RowStage<float, EMB>::kWords];
+    __shared__ uint4 tbl[kLevelTableMax + 2];
+    level_table_build(tbl, p);
+    __syncthreads();
+    float *stage = stage_cta + (threadIdx.x >> 5) * RowStage<float, EMB>::kWords;
+    const float *x = (const float *)p.x;
+    const int lane = threadIdx.x & 31;
+    const long long gwarp = (long long)blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);
+    const long long nwarps = (long long)gridDim.x * kWarpsPerCta;
+    const long long nc = p.nc;
+    const long long tau = p.tau;
+    const long long T_ = p.tbands, B = p.chunk;
+    const int shift = p.lt_shift, base = (int)p.lt_lo - 1, nb = p.lt_nb;
+
+    for (long long unit = gwarp; unit < p.nunits; unit += nwarps) {
+        const long long band = unit % T_, chunk = unit / T_;
+        const long long nblk = T_ - band;            // tiles (band, band..T-1)
+        const long long kb = chunk * B;
+        if (kb >= nblk) continue;                     // warp-uniform
+        const long long ke = kb + B < nblk ? kb + B : nblk;
+        const long long i = band * 32 + lane;
+        const bool row_ok = i < nc;
+        LaneVec<float, EMB> a;
+        a.load(x + i, tau);
+        u32 *dst = p.planes + tile_index(band, band, T_) * NP * 32 + lane;
+        for (long long k = kb; k < ke; k++) {
+            const long long j0 = (band + k) * 32;
+            const long long hi = nc - j0 < 32 ? nc - j0 : 32;
+            u32 P[NP];
+#pragma unroll
+            for (int b = 0; b < NP; b++) P[b] = 0;
+            if (k == 0 || hi < 32)   // the diagonal tile (cells j >= i) or the last column tile
+                row_planes_levels<NORM, EMB, true>(P, a, x + j0, tau, k == 0 ? lane : 0, hi,
+                                                   p.keys, stage, tbl, shift, base, nb);
+            else
+                row_planes_levels<NORM, EMB, false>(P, a, x + j0, tau, 0, 32, p.keys, stage, tbl,
+                                                    shift, base, nb);
+#pragma unroll
+            for (int b = 0; b < NP; b++) __stcg(dst + (k * NP + b) * 32, row_ok ? P[b] : 0u);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// det_diags by levels (float, fixed embedding, 16 slots, a bucket table):
+// det_diags' walk, staging and units, each block's cells given their levels
+// from the table and pushed into planes, the runs closed from the planes'
+// slot masks as the level walks close them.
+// ---------------------------------------------------------------------------
+template <int NORM, int EMB, bool CHECK>
+__device__ __forceinline__ void diag_planes_levels(u32 (&P)[Planes<16>::kN],
+                                                   const float *__restrict__ xs,
+                                                   const float *__restrict__ xsd, long long tau,
+                                                   long long rem,
+                                                   const u64 (&keys)[kMaxThrPerPass],
+                                                   float *stage, const uint4 *tbl, int shift,
+                                                   int base, int nb) {
+    constexpr int NP = Planes<16>::kN;
+    diag_stage<EMB>(stage, xs, xsd, tau);
+#pragma unroll 1
+    for (int g = 0; g < 32; g += kGroup) {
+        f2 v[kGroup / 2];
+        diag_group_staged<NORM, EMB, CHECK>(v, stage, g, rem);
+        u64 any = 0;
+#pragma unroll
+        for (int q = 0; q < kGroup / 2; q++) any |= sub2(v[q], keys[0]);
+        if (!__any_sync(0xFFFFFFFFu, ((u32)any | (u32)(any >> 32)) >> 31)) {
+#pragma unroll
+            for (int b = 0; b < NP; b++) P[b] <<= kGroup;   // level 0 everywhere
+            continue;
+        }
+        levels_push8<NP>(P, v, tbl, shift, base, nb);
+    }
+}
+
+template <int NORM, int EMB>
+__global__ void __launch_bounds__(kWarpsPerCta * 32, kDiagMinCtas)
+det_diags_lt(const __grid_constant__ WalkArgs p) {
+    constexpr int NT = kMaxThrPerPass, NP = Planes<NT>::kN;
+    extern __shared__ u32 smem[];
+    __shared__ __align__(16) float stage_cta[kWarpsPerCta * DiagStage<float, EMB>::kWords];
+    __shared__ uint4 tbl[kLevelTableMax + 2];
+    u32 *sh = smem;
+    u32 *shmax = smem + NT * kShortRunBins;
+    level_table_build(tbl, p);
+    hist_smem_clear(sh, shmax, NT * kShortRunBins);   // (synchronizes the CTA)
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float *stage = stage_cta + warp * DiagStage<float, EMB>::kWords;
+    HistSink sink{sh, shmax, p.hist, p.hist_stride, p.row, nullptr};
+    u32 carry[NT];
+    const float *x = (const float *)p.x;
+    const long long gwarp = (long long)blockIdx.x * kWarpsPerCta + warp;
+    const long long nwarps = (long long)gridDim.x * kWarpsPerCta;
+    const long long nc = p.nc;
+    const long long tau = p.tau;
+    const bool chunked = p.lead != nullptr;
+    const int shift = p.lt_shift, base = (int)p.lt_lo - 1, nb = p.lt_nb;
+
+    for (long long unit = gwarp; unit < p.nunits; unit += nwarps) {
+#pragma unroll 1
+        for (int half = 0; half < 2; half++) {
+            long long band, kb, ke;
+            if (chunked) {
+                if (half == 1) break;
+                band = unit % p.nbands;
+                const long long nbk = p.nbands - band;
+                const long long c = unit / p.nbands;
+                kb = c * p.chunk;
+                if (kb >= nbk) break;   // warp-uniform
+                ke = kb + p.chunk < nbk ? kb + p.chunk : nbk;
+                sink.lead = p.lead + line_record(true, p.nbands, p.chunk, c, band) * NT * 32 + lane;
+            } else {
+                band = half == 0 ? unit : p.nbands - 1 - unit;
+                if (half == 1 && band == unit) break;
+                kb = 0;
+                ke = p.nbands - band;
+            }
+            const long long d = 1 + band * 32 + lane;
+            const long long len = nc - d;                 // cells on this diagonal
+            const long long wmin = nc - (band * 32 + 32); // shortest diagonal of the warp
+            runs_begin<NT>(carry, chunked ? kRunSentinel : 0u);
+            long long s0 = kb * 32;
+            const long long se = ke * 32;
+            for (; s0 + 32 <= wmin && s0 < se; s0 += 32) {
+                u32 P[NP];
+#pragma unroll
+                for (int b = 0; b < NP; b++) P[b] = 0;
+                diag_planes_levels<NORM, EMB, false>(P, x + s0, x + s0 + d, tau, 32, p.keys,
+                                                     stage, tbl, shift, base, nb);
+                close_block_planes<NT, NP, HistSink>(P, carry, sink);
+            }
+            for (; s0 < se; s0 += 32) {
+                u32 P[NP];
+#pragma unroll
+                for (int b = 0; b < NP; b++) P[b] = 0;
+                diag_planes_levels<NORM, EMB, true>(P, x + s0, x + s0 + d, tau, len - s0, p.keys,
+                                                    stage, tbl, shift, base, nb);
+                close_block_planes<NT, NP, HistSink>(P, carry, sink);
+            }
+            if (chunked) {
+                runs_store<NT>(carry, p.trail + (sink.lead - p.lead));
+            } else {
+                runs_end<NT, HistSink>(carry, sink);
+            }
+        }
+    }
+    hist_smem_flush(sh, shmax, p);
+}
+
+// ---------------------------------------------------------------------------
 // lam_levels: lam_rows with masks from the planes.  Units, chunk records and
 // the stitch are lam_rows' (p.nbands = p.tbands row bands).
 // ---------------------------------------------------------------------------

@@ -25,6 +25,41 @@ constexpr u64 kNeverFilterPair = 0xFF800000FF800000ull;
 // pass kind read at run time); not a walk kind of the ABI.
 constexpr int kWalkLevels = 3;
 
+// Bucket table of an RR pass counted by level (rqa_level_table.cuh): the
+// coarsest shift at which no two different non-zero limits share a bucket,
+// if the buckets between the smallest and the largest limit fit the table.
+// a.keys holds the sorted float limit pairs (low 32 bits = the limit).
+static void plan_level_table(WalkArgs &a) {
+    a.lt_on = 0;
+    u32 lim[kMaxThrPerPass];
+    int nz = 0;
+    for (int k = 0; k < a.nthr; k++)
+        if ((u32)a.keys[k]) lim[nz++] = (u32)a.keys[k];   // decreasing
+    if (nz == 0) {   // no limit is ever met: every level is 0
+        a.lt_on = 1;
+        a.lt_shift = 31;
+        a.lt_lo = 0;
+        a.lt_nb = 0;
+        return;
+    }
+    for (int shift = 31; shift >= 1; shift--) {
+        bool distinct = true;
+        for (int k = 0; k + 1 < nz; k++)
+            if (lim[k] != lim[k + 1] && (lim[k] >> shift) == (lim[k + 1] >> shift)) {
+                distinct = false;
+                break;
+            }
+        if (!distinct) continue;
+        const u32 lo = lim[nz - 1] >> shift, hi = lim[0] >> shift;
+        if ((long long)(hi - lo) + 1 > kLevelTableMax) return;   // finer only grows
+        a.lt_on = 1;
+        a.lt_shift = shift;
+        a.lt_lo = lo;
+        a.lt_nb = (int)(hi - lo + 1);
+        return;
+    }
+}
+
 // The pass descriptor as kernel arguments: slots in decreasing threshold
 // order (see WalkArgs), the caller's order kept in row[], padding keys the
 // never-recurrent minimum.
@@ -68,6 +103,10 @@ static void fill_walk_args(const accrqa_walk_desc &d, WalkArgs &a) {
         }
         a.row[k] = order[k] < d.nthr ? order[k] : 0;
     }
+    // float passes of more than 8 thresholds: the bucket table of the RR
+    // and tile-level kernels that count or store cells by level
+    if (std::is_same<T, float>::value && d.dtype == ACCRQA_F32 && d.nthr > 8)
+        plan_level_table(a);
     a.xhi = (const float *)d.d_xhi;
     a.xlo = (const float *)d.d_xlo;
     a.counts = (u64 *)d.d_counts;
@@ -142,9 +181,19 @@ static cudaError_t launch_levels_one(const accrqa_walk_desc &d, cudaStream_t st)
     a.planes = (u32 *)d.d_planes;
     a.tbands = T_;
 
-    static std::atomic<int> c_tiles{-1}, c_det{-1}, c_lam{-1};
+    // float series with 16 slots whose limits admit a bucket table store
+    // their tile levels from the table (tile_levels_lt), the rest by slots
+    void (*tiles)(WalkArgs) = tile_levels<T, NORM, EMB, NT>;
+    static std::atomic<int> c_tiles{-1}, c_tiles_lt{-1}, c_det{-1}, c_lam{-1};
+    std::atomic<int> *c_t = &c_tiles;
+    if constexpr (std::is_same<T, float>::value && EMB > 0 && NT == kMaxThrPerPass) {
+        if (a.lt_on) {
+            tiles = tile_levels_lt<NORM, EMB>;
+            c_t = &c_tiles_lt;
+        }
+    }
     int per1 = 0, per2 = 0;
-    cudaError_t e = per_sm_of(tile_levels<T, NORM, EMB, NT>, 0, c_tiles, &per1);
+    cudaError_t e = per_sm_of(tiles, 0, *c_t, &per1);
     if (e != cudaSuccess) return e;
     void (*walk)(WalkArgs) = det ? det_levels<NT> : lam_levels<NT>;
     e = per_sm_of(walk, LineSmem<NT>::kBytes, det ? c_det : c_lam, &per2);
@@ -153,7 +202,7 @@ static cudaError_t launch_levels_one(const accrqa_walk_desc &d, cudaStream_t st)
     if (!d.planes_ready) {
         plan_upper_units(T_, (long long)sm_count_cached() * per1 * kWarpsPerCta, &a.chunk,
                          &a.nunits, accrqa_gb300_units_per_warp(ACCRQA_WALK_RR, d.nc));
-        tile_levels<T, NORM, EMB, NT><<<grid_for(a.nunits, per1), kWarpsPerCta * 32, 0, st>>>(a);
+        tiles<<<grid_for(a.nunits, per1), kWarpsPerCta * 32, 0, st>>>(a);
         g_launches.fetch_add(1);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
@@ -181,13 +230,14 @@ static cudaError_t launch_levels_one(const accrqa_walk_desc &d, cudaStream_t st)
 
 // Which RR walk a float pass takes.  The diagonal walk evaluates one
 // distance term per cell instead of emb, but its warp-wide skip groups are
-// less often empty than the row walk's 32 x 8 cell patches, so the threshold
-// work it saves on distances is partly spent again on compares.  Measured on
-// the GB300 (Lorenz x, N = 200,000, 16 thresholds, ms per pass, diagonal /
-// rows): tau 1: emb 3 22.4 / 17.6, emb 5 22.8 / 20.3, emb 8 20.4 / 24.6;
-// tau 2: 19.8 / 17.3, 19.2 / 19.4, 16.0 / 23.4; tau 4: 17.4 / 16.3,
-// 15.3 / 18.1, 13.1 / 22.5; tau 8: 15.6 / 14.9, 13.6 / 17.1, 12.1 / 21.7;
-// and with 4 thresholds (N = 1e6, tau 1, emb 5) 0.27 / 0.33 s.  The diagonal
+// less often empty than the row walk's 32 x 8 cell patches, so part of what
+// it saves on distances is spent again on threshold work.  Measured on the
+// GB300 (Lorenz x, N = 200,000, 16 thresholds counted by level, ms per pass,
+// diagonal / rows): tau 1: emb 3 18.8 / 13.0, emb 5 19.6 / 16.2, emb 8
+// 17.7 / 21.2; tau 2: 15.2 / 12.9, 15.6 / 15.7, 14.8 / 20.2; tau 4:
+// 14.4 / 12.5, 13.9 / 14.7, 13.0 / 19.2; tau 8: 13.5 / 11.4, 12.3 / 13.7,
+// 12.3 / 18.6 (with slot masks instead of levels the same crossover); and
+// with 4 thresholds (N = 1e6, tau 1, emb 5) 0.27 / 0.33 s.  The diagonal
 // walk wins once the term window spans (emb - 1) tau >= 7 positions with
 // emb >= 4, or with few thresholds, where the distance is most of the work.
 // Its 32-bit series indices need n + ACCRQA_SERIES_PAD < 2^31.
@@ -202,12 +252,22 @@ inline bool rr_along_diagonals(int emb, int tau, int nthr, long long nc) {
 // resident warp.
 template <int NORM, int EMB, int NT>
 static cudaError_t launch_rr_diag(const accrqa_walk_desc &d, cudaStream_t st) {
-    static std::atomic<int> c_diag{-1};
-    int per_sm = 0;
-    cudaError_t e = per_sm_of(rr_diags<NORM, EMB, NT>, 0, c_diag, &per_sm);
-    if (e != cudaSuccess) return e;
     WalkArgs a;
     fill_walk_args<float>(d, a);
+    // more than 8 thresholds: the cells are counted by level when the
+    // limits admit a bucket table
+    bool levels = false;
+    void (*kern)(WalkArgs) = rr_diags<NORM, EMB, NT, false>;
+    if constexpr (NT == kMaxThrPerPass) {
+        if (a.lt_on) {
+            levels = true;
+            kern = rr_diags<NORM, EMB, NT, true>;
+        }
+    }
+    static std::atomic<int> c_diag{-1}, c_diag_lv{-1};
+    int per_sm = 0;
+    cudaError_t e = per_sm_of(kern, 0, levels ? c_diag_lv : c_diag, &per_sm);
+    if (e != cudaSuccess) return e;
     const long long sms = sm_count_cached();
     long long g0 = (d.nc + 255) / 256;
     if (g0 > sms * 4) g0 = sms * 4;
@@ -233,7 +293,25 @@ static cudaError_t launch_rr_diag(const accrqa_walk_desc &d, cudaStream_t st) {
     if (C < 64) C = 64;
     a.chunk = C;
     a.nunits = a.nbands * ((d.nc - 1 + C - 1) / C);
-    rr_diags<NORM, EMB, NT><<<grid_for(a.nunits, per_sm), kWarpsPerCta * 32, 0, st>>>(a);
+    kern<<<grid_for(a.nunits, per_sm), kWarpsPerCta * 32, 0, st>>>(a);
+    g_launches.fetch_add(1);
+    return cudaGetLastError();
+}
+
+// RR of a float series with a fixed embedding along rows, counted by level
+// (16 slots with a bucket table; rr_rows' units).
+template <int NORM, int EMB>
+static cudaError_t launch_rr_rows_levels(const WalkArgs &a0, cudaStream_t st) {
+    static std::atomic<int> c_rows_lv{-1};
+    int per_sm = 0;
+    cudaError_t e = per_sm_of(rr_rows_levels<NORM, EMB>, 0, c_rows_lv, &per_sm);
+    if (e != cudaSuccess) return e;
+    WalkArgs a = a0;
+    a.nbands = (a.nc + 31) / 32;
+    plan_upper_units(a.nbands, (long long)sm_count_cached() * per_sm * kWarpsPerCta, &a.chunk,
+                     &a.nunits, accrqa_gb300_units_per_warp(ACCRQA_WALK_RR, a.nc));
+    if (a.nunits <= 0) return cudaSuccess;
+    rr_rows_levels<NORM, EMB><<<grid_for(a.nunits, per_sm), kWarpsPerCta * 32, 0, st>>>(a);
     g_launches.fetch_add(1);
     return cudaGetLastError();
 }
@@ -241,8 +319,14 @@ static cudaError_t launch_rr_diag(const accrqa_walk_desc &d, cudaStream_t st) {
 template <int KIND, typename T, int NORM, int EMB, int NT>
 static cudaError_t launch_one(const accrqa_walk_desc &d, cudaStream_t st) {
     if constexpr (KIND == kWalkLevels) return launch_levels_one<T, NORM, EMB, NT>(d, st);
-    if constexpr (KIND == ACCRQA_WALK_RR && std::is_same<T, float>::value && EMB > 0)
+    if constexpr (KIND == ACCRQA_WALK_RR && std::is_same<T, float>::value && EMB > 0) {
         if (rr_along_diagonals(EMB, d.tau, d.nthr, d.nc)) return launch_rr_diag<NORM, EMB, NT>(d, st);
+        if constexpr (NT == kMaxThrPerPass) {
+            WalkArgs a;
+            fill_walk_args<float>(d, a);
+            if (a.lt_on) return launch_rr_rows_levels<NORM, EMB>(a, st);
+        }
+    }
     void (*kern)(WalkArgs);
     size_t smem = 0;
     // if constexpr: a translation unit instantiates only its own kind
@@ -255,12 +339,21 @@ static cudaError_t launch_one(const accrqa_walk_desc &d, cudaStream_t st) {
         kern = lam_rows<T, NORM, EMB, NT>;
         smem = LineSmem<NT>::kBytes;
     }
-    static std::atomic<int> per_sm_cache{-1};
-    int per_sm = 0;
-    cudaError_t e0 = per_sm_of(kern, smem, per_sm_cache, &per_sm);
-    if (e0 != cudaSuccess) return e0;
     WalkArgs a;
     fill_walk_args<T>(d, a);
+    // DET of a float series with 16 slots and a bucket table: levels
+    static std::atomic<int> per_sm_cache{-1}, per_sm_cache_lt{-1};
+    std::atomic<int> *pc = &per_sm_cache;
+    if constexpr (KIND == ACCRQA_WALK_DET && std::is_same<T, float>::value && EMB > 0 &&
+                  NT == kMaxThrPerPass) {
+        if (a.lt_on) {
+            kern = det_diags_lt<NORM, EMB>;
+            pc = &per_sm_cache_lt;
+        }
+    }
+    int per_sm = 0;
+    cudaError_t e0 = per_sm_of(kern, smem, *pc, &per_sm);
+    if (e0 != cudaSuccess) return e0;
     LinePlan q{};
     if (KIND != ACCRQA_WALK_RR) {
         // chunked when the caller's scratch holds the boundary records

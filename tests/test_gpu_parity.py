@@ -127,6 +127,32 @@ def test_edge_series(gpu, oracle_mod, dt):
                     lam[k], oracle_mod.lam_hist(x, 1, emb, t, norm), err_msg=f"{name} LAM {t}")
 
 
+@pytest.mark.parametrize("norm", NORMS)
+def test_rr_level_table_thresholds(gpu, oracle_mod, norm):
+    """Float RR passes of more than 8 thresholds count cells by level from a
+    bucket table built from the thresholds' limits: negative, zero, tiny,
+    infinite and NaN thresholds, repeated ones, limits a few ulps apart
+    (fine buckets, or no table), limits spread over sixty decades, and a
+    series with NaN, inf and exactly tied distances -- on the row walk
+    (emb 2) and the diagonal walk (emb 4, tau 3)."""
+    x = workloads.logistic(900, 4).astype(np.float32)
+    x[:300] = np.round(x[:300] * 16) / 16
+    x[450], x[451], x[700] = np.nan, np.inf, -np.inf
+    sets = [
+        np.array([-1.0, -0.0, 0.0, 1e-30, 0.05, 0.05, 0.0625, 0.1, np.nextafter(0.1, 1.0),
+                  0.2, 0.25, 0.5, np.inf, np.nan], np.float32),
+        np.linspace(0.1, 0.1 + 15 * 2 ** -26, 16).astype(np.float32),
+        np.geomspace(1e-30, 1e30, 16).astype(np.float32),
+        np.full(16, 0.125, np.float32),
+        np.linspace(0.0, 0.9, 9).astype(np.float32),
+    ]
+    for thr in sets:
+        for tau, emb in [(1, 2), (3, 4)]:
+            np.testing.assert_array_equal(gpu.rr_counts(x, tau, emb, thr, norm),
+                                          oracle_mod.rr_counts(x, tau, emb, thr, norm),
+                                          err_msg=f"{thr} tau {tau} emb {emb}")
+
+
 @pytest.mark.parametrize("dt", [np.float32, np.float64])
 def test_rp_matches_oracle(gpu, oracle_mod, dt):
     x = workloads.lorenz_x(600, 3, transient=500).astype(dt)

@@ -181,7 +181,7 @@ def test_f64_filter_matches_oracle(gpu, oracle_mod, scale, offset, grid):
     x = x0 * scale + offset
     thr = np.array([0.0, 0.0625, 0.125, 0.3, 0.5, 0.75, 1.5]) * scale
     for norm in NORMS:
-        for tau, emb in [(1, 3), (2, 5), (1, 1)]:
+        for tau, emb in [(1, 3), (2, 5), (1, 1), (3, 4), (33, 4), (1, 8)]:
             np.testing.assert_array_equal(gpu.rr_counts(x, tau, emb, thr, norm),
                                           oracle_mod.rr_counts(x, tau, emb, thr, norm))
             det = gpu.det_histograms(x, tau, emb, thr, norm)

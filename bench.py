@@ -233,7 +233,10 @@ def run_ours(args):
 
     # the chunk granularity of the balanced walks, measured on this GPU
     # (about a second, before the warm-up and outside every timed region)
-    tuned = engine.autotune()
+    if args.no_autotune:
+        tuned = "off (built-in chunk granularity)"
+    else:
+        tuned = engine.autotune()
     log(f"autotune: {tuned}")
     log("inputs ready; warm-up")
     for _ in range(args.warmup):
@@ -792,6 +795,8 @@ def main(argv=None):
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the built-in chunk granularity (profiler launch lists)")
     ap.add_argument("--skip-batched", action="store_true")
     ap.add_argument("--skip-roofline-1m", action="store_true")
 

@@ -297,7 +297,86 @@ __device__ __forceinline__ void diag_planes_levels(u32 (&P)[Planes<16>::kN],
     }
 }
 
-template <int NORM, int EMB>
+// tau = 1: the terms of a diagonal, e(t) = (x[t] - x[t+d])^2 (|.| for the
+// maximal norm), are shared by emb consecutive cells -- cell s uses e(s) ..
+// e(s + emb - 1) -- so a group of 8 cells needs 8 new terms and keeps the last
+// emb - 1 in registers for the next group (tw).  Each cell's sum is still
+// formed in the reference's order, separately rounded.  The block stages only
+// the operands of its new terms (positions s0 + emb - 1 + c).
+template <int NORM, int EMB, bool CHECK>
+__device__ __forceinline__ void diag_planes_levels_tau1(u32 (&P)[Planes<16>::kN],
+                                                        float (&tw)[EMB > 1 ? EMB - 1 : 1],
+                                                        const float *__restrict__ xs,
+                                                        const float *__restrict__ xsd,
+                                                        long long rem,
+                                                        const u64 (&keys)[kMaxThrPerPass],
+                                                        float *stage, const uint4 *tbl, int shift,
+                                                        int base, int nb) {
+    constexpr int NP = Planes<16>::kN;
+    constexpr int H = EMB - 1;   // terms carried between groups
+    diag_stage<1>(stage, xs + H, xsd + H, 1);
+    const int lane = threadIdx.x & 31;
+    const f2 *stB = reinterpret_cast<const f2 *>(stage + 32);
+#pragma unroll 1
+    for (int g = 0; g < 32; g += kGroup) {
+        float T[H + kGroup];
+#pragma unroll
+        for (int m = 0; m < H; m++) T[m] = tw[m];
+#pragma unroll
+        for (int q = 0; q < kGroup / 2; q++) {
+            const int c = g + 2 * q;
+            const f2 dd = sub2(*reinterpret_cast<const f2 *>(stage + c), stB[lane + c]);
+            if (NORM == kNormEuclidean) {
+                T[H + 2 * q] = __fmul_rn(lo_of(dd), lo_of(dd));
+                T[H + 2 * q + 1] = __fmul_rn(hi_of(dd), hi_of(dd));
+            } else {
+                T[H + 2 * q] = fabsf(lo_of(dd));
+                T[H + 2 * q + 1] = fabsf(hi_of(dd));
+            }
+        }
+#pragma unroll
+        for (int m = 0; m < H; m++) tw[m] = T[kGroup + m];
+        f2 v[kGroup / 2];
+#pragma unroll
+        for (int q = 0; q < kGroup / 2; q++) {
+            float a0, a1;
+            if (NORM == kNormEuclidean) {
+                a0 = T[2 * q];                      // 0 + e == e exactly
+                a1 = T[2 * q + 1];
+#pragma unroll
+                for (int m = 1; m < EMB; m++) {
+                    a0 = __fadd_rn(a0, T[2 * q + m]);
+                    a1 = __fadd_rn(a1, T[2 * q + 1 + m]);
+                }
+            } else {
+                a0 = fmaxf(0.0f, T[2 * q]);         // "if (d > max) max = d" from 0
+                a1 = fmaxf(0.0f, T[2 * q + 1]);
+#pragma unroll
+                for (int m = 1; m < EMB; m++) {
+                    a0 = fmaxf(a0, T[2 * q + m]);
+                    a1 = fmaxf(a1, T[2 * q + 1 + m]);
+                }
+            }
+            if (CHECK) {
+                const int c = g + 2 * q;
+                a0 = (long long)c < rem ? a0 : never_value<float>();
+                a1 = (long long)c + 1 < rem ? a1 : never_value<float>();
+            }
+            v[q] = pack2(a0, a1);
+        }
+        u64 any = 0;
+#pragma unroll
+        for (int q = 0; q < kGroup / 2; q++) any |= sub2(v[q], keys[0]);
+        if (!__any_sync(0xFFFFFFFFu, ((u32)any | (u32)(any >> 32)) >> 31)) {
+#pragma unroll
+            for (int b = 0; b < NP; b++) P[b] <<= kGroup;   // level 0 everywhere
+            continue;
+        }
+        levels_push8<NP>(P, v, tbl, shift, base, nb);
+    }
+}
+
+template <int NORM, int EMB, bool TAU1 = false>
 __global__ void __launch_bounds__(kWarpsPerCta * 32, kDiagMinCtas)
 det_diags_lt(const __grid_constant__ WalkArgs p) {
     constexpr int NT = kMaxThrPerPass, NP = Planes<NT>::kN;
@@ -345,20 +424,37 @@ det_diags_lt(const __grid_constant__ WalkArgs p) {
             runs_begin<NT>(carry, chunked ? kRunSentinel : 0u);
             long long s0 = kb * 32;
             const long long se = ke * 32;
+            // tau = 1: the first cell's terms but the last, carried into the walk
+            float tw[EMB > 1 ? EMB - 1 : 1];
+            if constexpr (TAU1) {
+#pragma unroll
+                for (int m = 0; m + 1 < EMB; m++) {
+                    const float df = __fsub_rn(__ldg(x + s0 + m), __ldg(x + s0 + m + d));
+                    tw[m] = NORM == kNormEuclidean ? __fmul_rn(df, df) : fabsf(df);
+                }
+            }
             for (; s0 + 32 <= wmin && s0 < se; s0 += 32) {
                 u32 P[NP];
 #pragma unroll
                 for (int b = 0; b < NP; b++) P[b] = 0;
-                diag_planes_levels<NORM, EMB, false>(P, x + s0, x + s0 + d, tau, 32, p.keys,
-                                                     stage, tbl, shift, base, nb);
+                if constexpr (TAU1)
+                    diag_planes_levels_tau1<NORM, EMB, false>(P, tw, x + s0, x + s0 + d, 32,
+                                                              p.keys, stage, tbl, shift, base, nb);
+                else
+                    diag_planes_levels<NORM, EMB, false>(P, x + s0, x + s0 + d, tau, 32, p.keys,
+                                                         stage, tbl, shift, base, nb);
                 close_block_planes<NT, NP, HistSink>(P, carry, sink);
             }
             for (; s0 < se; s0 += 32) {
                 u32 P[NP];
 #pragma unroll
                 for (int b = 0; b < NP; b++) P[b] = 0;
-                diag_planes_levels<NORM, EMB, true>(P, x + s0, x + s0 + d, tau, len - s0, p.keys,
-                                                    stage, tbl, shift, base, nb);
+                if constexpr (TAU1)
+                    diag_planes_levels_tau1<NORM, EMB, true>(P, tw, x + s0, x + s0 + d, len - s0,
+                                                             p.keys, stage, tbl, shift, base, nb);
+                else
+                    diag_planes_levels<NORM, EMB, true>(P, x + s0, x + s0 + d, tau, len - s0,
+                                                        p.keys, stage, tbl, shift, base, nb);
                 close_block_planes<NT, NP, HistSink>(P, carry, sink);
             }
             if (chunked) {

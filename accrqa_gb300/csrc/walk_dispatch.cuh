@@ -342,13 +342,14 @@ static cudaError_t launch_one(const accrqa_walk_desc &d, cudaStream_t st) {
     WalkArgs a;
     fill_walk_args<T>(d, a);
     // DET of a float series with 16 slots and a bucket table: levels
-    static std::atomic<int> per_sm_cache{-1}, per_sm_cache_lt{-1};
+    // (tau = 1: the diagonal's distance terms carried between cells)
+    static std::atomic<int> per_sm_cache{-1}, per_sm_cache_lt{-1}, per_sm_cache_lt1{-1};
     std::atomic<int> *pc = &per_sm_cache;
     if constexpr (KIND == ACCRQA_WALK_DET && std::is_same<T, float>::value && EMB > 0 &&
                   NT == kMaxThrPerPass) {
         if (a.lt_on) {
-            kern = det_diags_lt<NORM, EMB>;
-            pc = &per_sm_cache_lt;
+            kern = d.tau == 1 ? det_diags_lt<NORM, EMB, true> : det_diags_lt<NORM, EMB, false>;
+            pc = d.tau == 1 ? &per_sm_cache_lt1 : &per_sm_cache_lt;
         }
     }
     int per_sm = 0;

@@ -297,23 +297,29 @@ __device__ __forceinline__ void diag_planes_levels(u32 (&P)[Planes<16>::kN],
     }
 }
 
-// tau = 1: the terms of a diagonal, e(t) = (x[t] - x[t+d])^2 (|.| for the
-// maximal norm), are shared by emb consecutive cells -- cell s uses e(s) ..
-// e(s + emb - 1) -- so a group of 8 cells needs 8 new terms and keeps the last
-// emb - 1 in registers for the next group (tw).  Each cell's sum is still
-// formed in the reference's order, separately rounded.  The block stages only
-// the operands of its new terms (positions s0 + emb - 1 + c).
-template <int NORM, int EMB, bool CHECK>
-__device__ __forceinline__ void diag_planes_levels_tau1(u32 (&P)[Planes<16>::kN],
-                                                        float (&tw)[EMB > 1 ? EMB - 1 : 1],
-                                                        const float *__restrict__ xs,
-                                                        const float *__restrict__ xsd,
-                                                        long long rem,
-                                                        const u64 (&keys)[kMaxThrPerPass],
-                                                        float *stage, const uint4 *tbl, int shift,
-                                                        int base, int nb) {
+// Small tau (TC = tau, a compile-time 1, 2 or 4): the terms of a diagonal,
+// e(t) = (x[t] - x[t+d])^2 (|.| for the maximal norm), are shared between
+// cells -- cell s uses e(s), e(s + tau), .., e(s + (emb-1) tau) -- so a group of
+// 8 cells needs 8 new terms and keeps the last H = (emb - 1) tau in registers
+// for the next group (tw).  Each cell's sum is still formed in the
+// reference's order, separately rounded.  The block stages only the operands
+// of its new terms (positions s0 + H + c).
+template <int TC, int EMB> struct TermWindow {
+    static constexpr int kH = TC * (EMB - 1);
+    static constexpr int kN = kH > 0 ? kH : 1;
+};
+
+template <int NORM, int EMB, int TC, bool CHECK>
+__device__ __forceinline__ void diag_planes_levels_tw(u32 (&P)[Planes<16>::kN],
+                                                      float (&tw)[TermWindow<TC, EMB>::kN],
+                                                      const float *__restrict__ xs,
+                                                      const float *__restrict__ xsd,
+                                                      long long rem,
+                                                      const u64 (&keys)[kMaxThrPerPass],
+                                                      float *stage, const uint4 *tbl, int shift,
+                                                      int base, int nb) {
     constexpr int NP = Planes<16>::kN;
-    constexpr int H = EMB - 1;   // terms carried between groups
+    constexpr int H = TermWindow<TC, EMB>::kH;   // terms carried between groups
     diag_stage<1>(stage, xs + H, xsd + H, 1);
     const int lane = threadIdx.x & 31;
     const f2 *stB = reinterpret_cast<const f2 *>(stage + 32);
@@ -345,16 +351,16 @@ __device__ __forceinline__ void diag_planes_levels_tau1(u32 (&P)[Planes<16>::kN]
                 a1 = T[2 * q + 1];
 #pragma unroll
                 for (int m = 1; m < EMB; m++) {
-                    a0 = __fadd_rn(a0, T[2 * q + m]);
-                    a1 = __fadd_rn(a1, T[2 * q + 1 + m]);
+                    a0 = __fadd_rn(a0, T[2 * q + m * TC]);
+                    a1 = __fadd_rn(a1, T[2 * q + 1 + m * TC]);
                 }
             } else {
                 a0 = fmaxf(0.0f, T[2 * q]);         // "if (d > max) max = d" from 0
                 a1 = fmaxf(0.0f, T[2 * q + 1]);
 #pragma unroll
                 for (int m = 1; m < EMB; m++) {
-                    a0 = fmaxf(a0, T[2 * q + m]);
-                    a1 = fmaxf(a1, T[2 * q + 1 + m]);
+                    a0 = fmaxf(a0, T[2 * q + m * TC]);
+                    a1 = fmaxf(a1, T[2 * q + 1 + m * TC]);
                 }
             }
             if (CHECK) {
@@ -376,8 +382,10 @@ __device__ __forceinline__ void diag_planes_levels_tau1(u32 (&P)[Planes<16>::kN]
     }
 }
 
-template <int NORM, int EMB, bool TAU1 = false>
-__global__ void __launch_bounds__(kWarpsPerCta * 32, kDiagMinCtas)
+// TC: 0 for any tau (operands staged per dimension), or the compile-time tau
+// of the carried-term walk.
+template <int NORM, int EMB, int TC = 0>
+__global__ void __launch_bounds__(kWarpsPerCta * 32, TC >= 4 ? kWideMinCtas : kDiagMinCtas)
 det_diags_lt(const __grid_constant__ WalkArgs p) {
     constexpr int NT = kMaxThrPerPass, NP = Planes<NT>::kN;
     extern __shared__ u32 smem[];
@@ -424,11 +432,12 @@ det_diags_lt(const __grid_constant__ WalkArgs p) {
             runs_begin<NT>(carry, chunked ? kRunSentinel : 0u);
             long long s0 = kb * 32;
             const long long se = ke * 32;
-            // tau = 1: the first cell's terms but the last, carried into the walk
-            float tw[EMB > 1 ? EMB - 1 : 1];
-            if constexpr (TAU1) {
+            // small tau: the terms of the H positions ahead of the first cell,
+            // carried into the walk
+            float tw[TermWindow<TC, EMB>::kN];
+            if constexpr (TC > 0) {
 #pragma unroll
-                for (int m = 0; m + 1 < EMB; m++) {
+                for (int m = 0; m < TermWindow<TC, EMB>::kH; m++) {
                     const float df = __fsub_rn(__ldg(x + s0 + m), __ldg(x + s0 + m + d));
                     tw[m] = NORM == kNormEuclidean ? __fmul_rn(df, df) : fabsf(df);
                 }
@@ -437,9 +446,9 @@ det_diags_lt(const __grid_constant__ WalkArgs p) {
                 u32 P[NP];
 #pragma unroll
                 for (int b = 0; b < NP; b++) P[b] = 0;
-                if constexpr (TAU1)
-                    diag_planes_levels_tau1<NORM, EMB, false>(P, tw, x + s0, x + s0 + d, 32,
-                                                              p.keys, stage, tbl, shift, base, nb);
+                if constexpr (TC > 0)
+                    diag_planes_levels_tw<NORM, EMB, TC, false>(P, tw, x + s0, x + s0 + d, 32,
+                                                                p.keys, stage, tbl, shift, base, nb);
                 else
                     diag_planes_levels<NORM, EMB, false>(P, x + s0, x + s0 + d, tau, 32, p.keys,
                                                          stage, tbl, shift, base, nb);
@@ -449,9 +458,9 @@ det_diags_lt(const __grid_constant__ WalkArgs p) {
                 u32 P[NP];
 #pragma unroll
                 for (int b = 0; b < NP; b++) P[b] = 0;
-                if constexpr (TAU1)
-                    diag_planes_levels_tau1<NORM, EMB, true>(P, tw, x + s0, x + s0 + d, len - s0,
-                                                             p.keys, stage, tbl, shift, base, nb);
+                if constexpr (TC > 0)
+                    diag_planes_levels_tw<NORM, EMB, TC, true>(P, tw, x + s0, x + s0 + d, len - s0,
+                                                               p.keys, stage, tbl, shift, base, nb);
                 else
                     diag_planes_levels<NORM, EMB, true>(P, x + s0, x + s0 + d, tau, len - s0,
                                                         p.keys, stage, tbl, shift, base, nb);

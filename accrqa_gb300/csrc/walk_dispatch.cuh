@@ -18,6 +18,12 @@ namespace accrqa {
 int sm_count_cached();
 extern std::atomic<unsigned long long> g_launches;
 
+// DET by levels with the diagonal's distance terms carried in registers
+// (det_diags_lt<NORM, EMB, TC>, TC = tau) for the taus and embeddings whose
+// term window (emb - 1) tau fits: the kernel, or null (walk_det_tw_f32.cu).
+constexpr int kDetTermWindowTaus = 8;
+void (*det_lt_term_window_kernel(int norm, int emb, int tau))(WalkArgs);
+
 // Filter limit pair of a padding slot: (-inf, -inf), surely not recurrent.
 constexpr u64 kNeverFilterPair = 0xFF800000FF800000ull;
 
@@ -342,14 +348,23 @@ static cudaError_t launch_one(const accrqa_walk_desc &d, cudaStream_t st) {
     WalkArgs a;
     fill_walk_args<T>(d, a);
     // DET of a float series with 16 slots and a bucket table: levels
-    // (tau = 1: the diagonal's distance terms carried between cells)
-    static std::atomic<int> per_sm_cache{-1}, per_sm_cache_lt{-1}, per_sm_cache_lt1{-1};
+    // (small tau: the diagonal's distance terms carried between cells, kernels
+    // instantiated in walk_det_tw_f32.cu)
+    static std::atomic<int> per_sm_cache{-1}, per_sm_cache_lt{-1};
+    static std::atomic<int> per_sm_cache_tw[kDetTermWindowTaus + 1] = {
+        {-1}, {-1}, {-1}, {-1}, {-1}, {-1}, {-1}, {-1}, {-1}};
     std::atomic<int> *pc = &per_sm_cache;
     if constexpr (KIND == ACCRQA_WALK_DET && std::is_same<T, float>::value && EMB > 0 &&
                   NT == kMaxThrPerPass) {
         if (a.lt_on) {
-            kern = d.tau == 1 ? det_diags_lt<NORM, EMB, true> : det_diags_lt<NORM, EMB, false>;
-            pc = d.tau == 1 ? &per_sm_cache_lt1 : &per_sm_cache_lt;
+            void (*tw)(WalkArgs) = det_lt_term_window_kernel(NORM, EMB, d.tau);
+            if (tw) {
+                kern = tw;
+                pc = &per_sm_cache_tw[d.tau];   // (non-null only for tau <= 8)
+            } else {
+                kern = det_diags_lt<NORM, EMB, 0>;
+                pc = &per_sm_cache_lt;
+            }
         }
     }
     int per_sm = 0;

@@ -300,6 +300,86 @@ __device__ __forceinline__ void diag_stage(float *stage, const float *__restrict
     __syncwarp();
 }
 
+// Small tau (TC = tau, a compile-time 1, 2 or 4): the terms of a diagonal,
+// e(t) = (x[t] - x[t+d])^2 (|.| for the maximal norm), are shared between
+// cells -- cell s uses e(s), e(s + tau), .., e(s + (emb-1) tau) -- so a group of
+// 8 cells needs 8 new terms and keeps the last H = (emb - 1) tau in registers
+// for the next group (tw).  Each cell's sum is still formed in the
+// reference's order, separately rounded.  The block stages only the operands
+// of its new terms (positions s0 + H + c).
+template <int TC, int EMB> struct TermWindow {
+    static constexpr int kH = TC * (EMB - 1);
+    static constexpr int kN = kH > 0 ? kH : 1;
+};
+
+// One group of 8 cells of the carried-term walk: its 8 new terms from the
+// block's stage (diag_stage<1> at positions s0 + H + c), the group's values
+// (cells past `rem` never recurrent), and the last H terms kept in tw.
+template <int NORM, int EMB, int TC, bool CHECK>
+__device__ __forceinline__ void tw_group_values(f2 (&v)[kGroup / 2],
+                                                float (&tw)[TermWindow<TC, EMB>::kN],
+                                                const float *stage, int g, long long rem) {
+    constexpr int H = TermWindow<TC, EMB>::kH;
+    const int lane = threadIdx.x & 31;
+    const f2 *stB = reinterpret_cast<const f2 *>(stage + 32);
+    float T[H + kGroup];
+#pragma unroll
+    for (int m = 0; m < H; m++) T[m] = tw[m];
+#pragma unroll
+    for (int q = 0; q < kGroup / 2; q++) {
+        const int c = g + 2 * q;
+        const f2 dd = sub2(*reinterpret_cast<const f2 *>(stage + c), stB[lane + c]);
+        if (NORM == kNormEuclidean) {
+            T[H + 2 * q] = __fmul_rn(lo_of(dd), lo_of(dd));
+            T[H + 2 * q + 1] = __fmul_rn(hi_of(dd), hi_of(dd));
+        } else {
+            T[H + 2 * q] = fabsf(lo_of(dd));
+            T[H + 2 * q + 1] = fabsf(hi_of(dd));
+        }
+    }
+#pragma unroll
+    for (int m = 0; m < H; m++) tw[m] = T[kGroup + m];
+#pragma unroll
+    for (int q = 0; q < kGroup / 2; q++) {
+        float a0, a1;
+        if (NORM == kNormEuclidean) {
+            a0 = T[2 * q];                      // 0 + e == e exactly
+            a1 = T[2 * q + 1];
+#pragma unroll
+            for (int m = 1; m < EMB; m++) {
+                a0 = __fadd_rn(a0, T[2 * q + m * TC]);
+                a1 = __fadd_rn(a1, T[2 * q + 1 + m * TC]);
+            }
+        } else {
+            a0 = fmaxf(0.0f, T[2 * q]);         // "if (d > max) max = d" from 0
+            a1 = fmaxf(0.0f, T[2 * q + 1]);
+#pragma unroll
+            for (int m = 1; m < EMB; m++) {
+                a0 = fmaxf(a0, T[2 * q + m * TC]);
+                a1 = fmaxf(a1, T[2 * q + 1 + m * TC]);
+            }
+        }
+        if (CHECK) {
+            const int c = g + 2 * q;
+            a0 = (long long)c < rem ? a0 : never_value<float>();
+            a1 = (long long)c + 1 < rem ? a1 : never_value<float>();
+        }
+        v[q] = pack2(a0, a1);
+    }
+}
+
+// The terms of the H positions ahead of a line's (or chunk's) first cell.
+template <int NORM, int EMB, int TC>
+__device__ __forceinline__ void tw_begin(float (&tw)[TermWindow<TC, EMB>::kN],
+                                         const float *__restrict__ x, long long s0, long long d) {
+#pragma unroll
+    for (int m = 0; m < TermWindow<TC, EMB>::kH; m++) {
+        const float df = __fsub_rn(__ldg(x + s0 + m), __ldg(x + s0 + m + d));
+        tw[m] = NORM == kNormEuclidean ? __fmul_rn(df, df) : fabsf(df);
+    }
+}
+
+
 template <int NORM, int EMB, bool CHECK>
 __device__ __forceinline__ void diag_group_staged(f2 (&v)[kGroup / 2], const float *stage, int g,
                                                   long long rem) {
@@ -611,6 +691,25 @@ __device__ __forceinline__ void diag_masks(u32 (&m)[NT], typename SeriesOf<T>::p
         } else {
             push_group<NT>(m, v, keys);
         }
+    }
+}
+
+// The masks of one 32-cell block of a diagonal by the carried-term walk
+// (float, compile-time tau TC; tw carries the window between blocks).
+template <int NORM, int EMB, int NT, int TC, bool CHECK>
+__device__ __forceinline__ void diag_masks_tw(u32 (&m)[NT], float (&tw)[TermWindow<TC, EMB>::kN],
+                                              const float *__restrict__ xs,
+                                              const float *__restrict__ xsd, long long rem,
+                                              const u64 (&keys)[kMaxThrPerPass], float *stage) {
+    constexpr int H = TermWindow<TC, EMB>::kH;
+#pragma unroll
+    for (int k = 0; k < NT; k++) m[k] = 0;
+    diag_stage<1>(stage, xs + H, xsd + H, 1);
+#pragma unroll 1
+    for (int g = 0; g < 32; g += kGroup) {
+        f2 v[kGroup / 2];
+        tw_group_values<NORM, EMB, TC, CHECK>(v, tw, stage, g, rem);
+        push_group<NT>(m, v, keys);
     }
 }
 
@@ -941,7 +1040,9 @@ __device__ __forceinline__ void det_block(typename SeriesOf<T>::ptr xs,
     close_block<NT, Sink>(m, carry, sink);
 }
 
-template <typename T, int NORM, int EMB, int NT>
+// TC > 0 (float, compile-time tau): the diagonal's distance terms carried
+// between cells (tw_group_values) instead of every dimension staged.
+template <typename T, int NORM, int EMB, int NT, int TC = 0>
 __global__ void __launch_bounds__(kWarpsPerCta * 32, kDiagMinCtas)
 det_diags(const __grid_constant__ WalkArgs p) {
     extern __shared__ u32 smem[];
@@ -989,12 +1090,30 @@ det_diags(const __grid_constant__ WalkArgs p) {
             runs_begin<NT>(carry, chunked ? kRunSentinel : 0u);
             long long s0 = kb * 32;
             const long long se = ke * 32;
-            for (; s0 + 32 <= wmin && s0 < se; s0 += 32)
-                det_block<T, NORM, EMB, NT, false>(x + s0, x + s0 + d, tau, p.emb, 32, p.keys, xkeys,
-                                                   carry, sink, stage);
-            for (; s0 < se; s0 += 32)
-                det_block<T, NORM, EMB, NT, true>(x + s0, x + s0 + d, tau, p.emb, len - s0,
-                                                  p.keys, xkeys, carry, sink, stage);
+            if constexpr (TC > 0) {
+                float tw[TermWindow<TC, EMB>::kN];
+                tw_begin<NORM, EMB, TC>(tw, (const float *)p.x, s0, d);
+                const float *xf = (const float *)p.x;
+                for (; s0 + 32 <= wmin && s0 < se; s0 += 32) {
+                    u32 m[NT];
+                    diag_masks_tw<NORM, EMB, NT, TC, false>(m, tw, xf + s0, xf + s0 + d, 32,
+                                                            p.keys, stage);
+                    close_block<NT, HistSink>(m, carry, sink);
+                }
+                for (; s0 < se; s0 += 32) {
+                    u32 m[NT];
+                    diag_masks_tw<NORM, EMB, NT, TC, true>(m, tw, xf + s0, xf + s0 + d, len - s0,
+                                                           p.keys, stage);
+                    close_block<NT, HistSink>(m, carry, sink);
+                }
+            } else {
+                for (; s0 + 32 <= wmin && s0 < se; s0 += 32)
+                    det_block<T, NORM, EMB, NT, false>(x + s0, x + s0 + d, tau, p.emb, 32, p.keys,
+                                                       xkeys, carry, sink, stage);
+                for (; s0 < se; s0 += 32)
+                    det_block<T, NORM, EMB, NT, true>(x + s0, x + s0 + d, tau, p.emb, len - s0,
+                                                      p.keys, xkeys, carry, sink, stage);
+            }
             if (chunked) {
                 runs_store<NT>(carry, p.trail + (sink.lead - p.lead));
             } else {

@@ -297,18 +297,6 @@ __device__ __forceinline__ void diag_planes_levels(u32 (&P)[Planes<16>::kN],
     }
 }
 
-// Small tau (TC = tau, a compile-time 1, 2 or 4): the terms of a diagonal,
-// e(t) = (x[t] - x[t+d])^2 (|.| for the maximal norm), are shared between
-// cells -- cell s uses e(s), e(s + tau), .., e(s + (emb-1) tau) -- so a group of
-// 8 cells needs 8 new terms and keeps the last H = (emb - 1) tau in registers
-// for the next group (tw).  Each cell's sum is still formed in the
-// reference's order, separately rounded.  The block stages only the operands
-// of its new terms (positions s0 + H + c).
-template <int TC, int EMB> struct TermWindow {
-    static constexpr int kH = TC * (EMB - 1);
-    static constexpr int kN = kH > 0 ? kH : 1;
-};
-
 template <int NORM, int EMB, int TC, bool CHECK>
 __device__ __forceinline__ void diag_planes_levels_tw(u32 (&P)[Planes<16>::kN],
                                                       float (&tw)[TermWindow<TC, EMB>::kN],
@@ -321,55 +309,10 @@ __device__ __forceinline__ void diag_planes_levels_tw(u32 (&P)[Planes<16>::kN],
     constexpr int NP = Planes<16>::kN;
     constexpr int H = TermWindow<TC, EMB>::kH;   // terms carried between groups
     diag_stage<1>(stage, xs + H, xsd + H, 1);
-    const int lane = threadIdx.x & 31;
-    const f2 *stB = reinterpret_cast<const f2 *>(stage + 32);
 #pragma unroll 1
     for (int g = 0; g < 32; g += kGroup) {
-        float T[H + kGroup];
-#pragma unroll
-        for (int m = 0; m < H; m++) T[m] = tw[m];
-#pragma unroll
-        for (int q = 0; q < kGroup / 2; q++) {
-            const int c = g + 2 * q;
-            const f2 dd = sub2(*reinterpret_cast<const f2 *>(stage + c), stB[lane + c]);
-            if (NORM == kNormEuclidean) {
-                T[H + 2 * q] = __fmul_rn(lo_of(dd), lo_of(dd));
-                T[H + 2 * q + 1] = __fmul_rn(hi_of(dd), hi_of(dd));
-            } else {
-                T[H + 2 * q] = fabsf(lo_of(dd));
-                T[H + 2 * q + 1] = fabsf(hi_of(dd));
-            }
-        }
-#pragma unroll
-        for (int m = 0; m < H; m++) tw[m] = T[kGroup + m];
         f2 v[kGroup / 2];
-#pragma unroll
-        for (int q = 0; q < kGroup / 2; q++) {
-            float a0, a1;
-            if (NORM == kNormEuclidean) {
-                a0 = T[2 * q];                      // 0 + e == e exactly
-                a1 = T[2 * q + 1];
-#pragma unroll
-                for (int m = 1; m < EMB; m++) {
-                    a0 = __fadd_rn(a0, T[2 * q + m * TC]);
-                    a1 = __fadd_rn(a1, T[2 * q + 1 + m * TC]);
-                }
-            } else {
-                a0 = fmaxf(0.0f, T[2 * q]);         // "if (d > max) max = d" from 0
-                a1 = fmaxf(0.0f, T[2 * q + 1]);
-#pragma unroll
-                for (int m = 1; m < EMB; m++) {
-                    a0 = fmaxf(a0, T[2 * q + m * TC]);
-                    a1 = fmaxf(a1, T[2 * q + 1 + m * TC]);
-                }
-            }
-            if (CHECK) {
-                const int c = g + 2 * q;
-                a0 = (long long)c < rem ? a0 : never_value<float>();
-                a1 = (long long)c + 1 < rem ? a1 : never_value<float>();
-            }
-            v[q] = pack2(a0, a1);
-        }
+        tw_group_values<NORM, EMB, TC, CHECK>(v, tw, stage, g, rem);
         u64 any = 0;
 #pragma unroll
         for (int q = 0; q < kGroup / 2; q++) any |= sub2(v[q], keys[0]);
@@ -435,13 +378,7 @@ det_diags_lt(const __grid_constant__ WalkArgs p) {
             // small tau: the terms of the H positions ahead of the first cell,
             // carried into the walk
             float tw[TermWindow<TC, EMB>::kN];
-            if constexpr (TC > 0) {
-#pragma unroll
-                for (int m = 0; m < TermWindow<TC, EMB>::kH; m++) {
-                    const float df = __fsub_rn(__ldg(x + s0 + m), __ldg(x + s0 + m + d));
-                    tw[m] = NORM == kNormEuclidean ? __fmul_rn(df, df) : fabsf(df);
-                }
-            }
+            if constexpr (TC > 0) tw_begin<NORM, EMB, TC>(tw, x, s0, d);
             for (; s0 + 32 <= wmin && s0 < se; s0 += 32) {
                 u32 P[NP];
 #pragma unroll

@@ -1,7 +1,8 @@
-// Kernel instantiations of DET by levels with the distance terms carried
-// between cells (float series, 16 slots, tau 1, 2, 4, and 8 up to emb 5:
-// term windows (emb - 1) tau of at most 32 positions), in a translation unit
-// of their own so that they compile beside the other DET kernels.
+// Kernel instantiations of DET with the distance terms carried between cells
+// (float series): by levels (16 slots) for tau 1, 2, 4, and 8 up to emb 5 --
+// term windows (emb - 1) tau of at most 32 positions -- and by slot masks (4
+// or 8 slots) for tau 1; in a translation unit of their own so that they
+// compile beside the other DET kernels.
 #include "walk_dispatch.cuh"
 
 namespace accrqa {
@@ -37,6 +38,38 @@ static void (*tw_for_emb(int emb, int tau))(WalkArgs) {
 void (*det_lt_term_window_kernel(int norm, int emb, int tau))(WalkArgs) {
     if (norm == kNormEuclidean) return tw_for_emb<kNormEuclidean>(emb, tau);
     if (norm == kNormMaximal) return tw_for_emb<kNormMaximal>(emb, tau);
+    return nullptr;
+}
+
+// DET by slot masks (4 or 8 thresholds) with carried terms, tau 1.
+template <int NORM, int EMB>
+static void (*masks_for_nt(int nt))(WalkArgs) {
+    switch (nt) {
+        case 4: return det_diags<float, NORM, EMB, 4, 1>;
+        case 8: return det_diags<float, NORM, EMB, 8, 1>;
+        default: return nullptr;
+    }
+}
+
+template <int NORM>
+static void (*masks_for_emb(int emb, int nt))(WalkArgs) {
+    switch (emb) {
+        case 1: return masks_for_nt<NORM, 1>(nt);
+        case 2: return masks_for_nt<NORM, 2>(nt);
+        case 3: return masks_for_nt<NORM, 3>(nt);
+        case 4: return masks_for_nt<NORM, 4>(nt);
+        case 5: return masks_for_nt<NORM, 5>(nt);
+        case 6: return masks_for_nt<NORM, 6>(nt);
+        case 7: return masks_for_nt<NORM, 7>(nt);
+        case 8: return masks_for_nt<NORM, 8>(nt);
+        default: return nullptr;
+    }
+}
+
+void (*det_masks_term_window_kernel(int norm, int emb, int nt, int tau))(WalkArgs) {
+    if (tau != 1) return nullptr;
+    if (norm == kNormEuclidean) return masks_for_emb<kNormEuclidean>(emb, nt);
+    if (norm == kNormMaximal) return masks_for_emb<kNormMaximal>(emb, nt);
     return nullptr;
 }
 

@@ -23,6 +23,9 @@ extern std::atomic<unsigned long long> g_launches;
 // term window (emb - 1) tau fits: the kernel, or null (walk_det_tw_f32.cu).
 constexpr int kDetTermWindowTaus = 8;
 void (*det_lt_term_window_kernel(int norm, int emb, int tau))(WalkArgs);
+// The same for DET by slot masks (4 or 8 slots; tau 1): det_diags<float, NORM,
+// EMB, NT, 1>, or null.
+void (*det_masks_term_window_kernel(int norm, int emb, int nt, int tau))(WalkArgs);
 
 // Filter limit pair of a padding slot: (-inf, -inf), surely not recurrent.
 constexpr u64 kNeverFilterPair = 0xFF800000FF800000ull;
@@ -365,6 +368,15 @@ static cudaError_t launch_one(const accrqa_walk_desc &d, cudaStream_t st) {
                 kern = det_diags_lt<NORM, EMB, 0>;
                 pc = &per_sm_cache_lt;
             }
+        }
+    }
+    if constexpr (KIND == ACCRQA_WALK_DET && std::is_same<T, float>::value && EMB > 0 &&
+                  NT < kMaxThrPerPass) {
+        static std::atomic<int> per_sm_cache_mtw{-1};
+        void (*tw)(WalkArgs) = det_masks_term_window_kernel(NORM, EMB, NT, d.tau);
+        if (tw) {
+            kern = tw;
+            pc = &per_sm_cache_mtw;
         }
     }
     int per_sm = 0;

@@ -713,6 +713,94 @@ __device__ __forceinline__ void diag_masks_tw(u32 (&m)[NT], float (&tw)[TermWind
     }
 }
 
+// float64 through the float filter, carried terms: the float term of a
+// position, ((h[t] - h[t+d]) + (l[t] - l[t+d]))^2, is exactly what the staged
+// filter evaluates for every cell and dimension that uses it, so the host's
+// bound holds; the stage is diag_stage_f64f<1> at positions s0 + H + c.
+template <int NORM, int EMB, int TC, bool CHECK>
+__device__ __forceinline__ void tw_group_values_f64f(f2 (&v)[kGroup / 2],
+                                                     float (&tw)[TermWindow<TC, EMB>::kN],
+                                                     const float *stage, int g, long long rem) {
+    constexpr int H = TermWindow<TC, EMB>::kH;
+    const int lane = threadIdx.x & 31;
+    float T[H + kGroup];
+#pragma unroll
+    for (int m = 0; m < H; m++) T[m] = tw[m];
+#pragma unroll
+    for (int q = 0; q < kGroup / 2; q++) {
+        const int c = g + 2 * q, w = lane + c;
+        const f2 dh = sub2(*reinterpret_cast<const f2 *>(stage + c),
+                           pack2(stage[64 + w], stage[64 + w + 1]));
+        const f2 dl = sub2(*reinterpret_cast<const f2 *>(stage + 32 + c),
+                           pack2(stage[128 + w], stage[128 + w + 1]));
+        const f2 dd = add2(dh, dl);
+        const f2 e = NORM == kNormEuclidean ? mul2(dd, dd)
+                                            : pack2(fabsf(lo_of(dd)), fabsf(hi_of(dd)));
+        T[H + 2 * q] = lo_of(e);
+        T[H + 2 * q + 1] = hi_of(e);
+    }
+#pragma unroll
+    for (int m = 0; m < H; m++) tw[m] = T[kGroup + m];
+#pragma unroll
+    for (int q = 0; q < kGroup / 2; q++) {
+        float a0 = T[2 * q], a1 = T[2 * q + 1];
+        if (NORM != kNormEuclidean) {
+            a0 = fmaxf(0.0f, a0);
+            a1 = fmaxf(0.0f, a1);
+        }
+#pragma unroll
+        for (int m = 1; m < EMB; m++) {
+            if (NORM == kNormEuclidean) {
+                a0 = a0 + T[2 * q + m * TC];   // inside the filter's bound, fused or not
+                a1 = a1 + T[2 * q + 1 + m * TC];
+            } else {
+                a0 = fmaxf(a0, T[2 * q + m * TC]);
+                a1 = fmaxf(a1, T[2 * q + 1 + m * TC]);
+            }
+        }
+        if (CHECK) {
+            const int c = g + 2 * q;
+            a0 = (long long)c < rem ? a0 : never_value<float>();
+            a1 = (long long)c + 1 < rem ? a1 : never_value<float>();
+        }
+        v[q] = pack2(a0, a1);
+    }
+}
+
+template <int NORM, int EMB, int TC>
+__device__ __forceinline__ void tw_begin_f64f(float (&tw)[TermWindow<TC, EMB>::kN], F64FPtr x,
+                                              long long s0, long long d) {
+#pragma unroll
+    for (int m = 0; m < TermWindow<TC, EMB>::kH; m++) {
+        const long long t = s0 + m;
+        const float df = (__ldg(x.h + t) - __ldg(x.h + t + d)) + (__ldg(x.l + t) - __ldg(x.l + t + d));
+        tw[m] = NORM == kNormEuclidean ? df * df : fabsf(df);
+    }
+}
+
+// The masks of one 32-cell block of a diagonal, float64 filter, carried
+// terms; ambiguous cells decided again in float64 (exact_fixup).
+template <int NORM, int EMB, int NT, int TC, bool CHECK>
+__device__ __forceinline__ void diag_masks_tw_f64f(u32 (&m)[NT],
+                                                   float (&tw)[TermWindow<TC, EMB>::kN],
+                                                   F64FPtr xs, F64FPtr xsd, long long tau,
+                                                   long long rem,
+                                                   const u64 (&keys)[kMaxThrPerPass],
+                                                   const u64 *xkeys, float *stage) {
+    constexpr int H = TermWindow<TC, EMB>::kH;
+#pragma unroll
+    for (int k = 0; k < NT; k++) m[k] = 0;
+    diag_stage_f64f<1>(stage, xs + H, xsd + H, 1);
+#pragma unroll 1
+    for (int g = 0; g < 32; g += kGroup) {
+        f2 v[kGroup / 2];
+        tw_group_values_f64f<NORM, EMB, TC, CHECK>(v, tw, stage, g, rem);
+        const u32 amb = push_group_filtered<NT>(m, v, keys);
+        if (__any_sync(0xFFFFFFFFu, amb != 0u))
+            exact_fixup<NORM, EMB, NT>(m, amb, xs.d + g, 1, xsd.d + g, tau, EMB, xkeys);
+    }
+}
+
 // Shared-memory histogram set-up and flush, shared by the line kernels.
 __device__ __forceinline__ void hist_smem_clear(u32 *sh, u32 *shmax, int nbins) {
     for (int t = threadIdx.x; t < nbins; t += blockDim.x) sh[t] = 0;
@@ -1090,7 +1178,22 @@ det_diags(const __grid_constant__ WalkArgs p) {
             runs_begin<NT>(carry, chunked ? kRunSentinel : 0u);
             long long s0 = kb * 32;
             const long long se = ke * 32;
-            if constexpr (TC > 0) {
+            if constexpr (TC > 0 && std::is_same<T, F64F>::value) {
+                float tw[TermWindow<TC, EMB>::kN];
+                tw_begin_f64f<NORM, EMB, TC>(tw, x, s0, d);
+                for (; s0 + 32 <= wmin && s0 < se; s0 += 32) {
+                    u32 m[NT];
+                    diag_masks_tw_f64f<NORM, EMB, NT, TC, false>(m, tw, x + s0, x + s0 + d, tau,
+                                                                 32, p.keys, xkeys, stage);
+                    close_block<NT, HistSink>(m, carry, sink);
+                }
+                for (; s0 < se; s0 += 32) {
+                    u32 m[NT];
+                    diag_masks_tw_f64f<NORM, EMB, NT, TC, true>(m, tw, x + s0, x + s0 + d, tau,
+                                                                len - s0, p.keys, xkeys, stage);
+                    close_block<NT, HistSink>(m, carry, sink);
+                }
+            } else if constexpr (TC > 0) {
                 float tw[TermWindow<TC, EMB>::kN];
                 tw_begin<NORM, EMB, TC>(tw, (const float *)p.x, s0, d);
                 const float *xf = (const float *)p.x;

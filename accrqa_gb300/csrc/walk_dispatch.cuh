@@ -26,6 +26,8 @@ void (*det_lt_term_window_kernel(int norm, int emb, int tau))(WalkArgs);
 // The same for DET by slot masks (4 or 8 slots; tau 1): det_diags<float, NORM,
 // EMB, NT, 1>, or null.
 void (*det_masks_term_window_kernel(int norm, int emb, int nt, int tau))(WalkArgs);
+// The same for float64 series through the float filter (walk_det_tw_f64f.cu).
+void (*det_f64f_term_window_kernel(int norm, int emb, int nt, int tau))(WalkArgs);
 
 // Filter limit pair of a padding slot: (-inf, -inf), surely not recurrent.
 constexpr u64 kNeverFilterPair = 0xFF800000FF800000ull;
@@ -370,10 +372,12 @@ static cudaError_t launch_one(const accrqa_walk_desc &d, cudaStream_t st) {
             }
         }
     }
-    if constexpr (KIND == ACCRQA_WALK_DET && std::is_same<T, float>::value && EMB > 0 &&
-                  NT < kMaxThrPerPass) {
+    if constexpr (KIND == ACCRQA_WALK_DET && EMB > 0 && NT < kMaxThrPerPass &&
+                  (std::is_same<T, float>::value || std::is_same<T, F64F>::value)) {
         static std::atomic<int> per_sm_cache_mtw{-1};
-        void (*tw)(WalkArgs) = det_masks_term_window_kernel(NORM, EMB, NT, d.tau);
+        void (*tw)(WalkArgs) = std::is_same<T, float>::value
+                                   ? det_masks_term_window_kernel(NORM, EMB, NT, d.tau)
+                                   : det_f64f_term_window_kernel(NORM, EMB, NT, d.tau);
         if (tw) {
             kern = tw;
             pc = &per_sm_cache_mtw;

@@ -172,19 +172,21 @@ __device__ __forceinline__ void diag_rr_flush(u32 (&m)[NT], u32 *cnt, bool on) {
     }
 }
 
-// Main diagonal: one thread per cell, counted once.
-template <int NORM, int EMB, int NT>
+// Main diagonal: one thread per cell, counted once.  T = double decides a
+// float64 series exactly against its exact limits (p.xkeys).
+template <int NORM, int EMB, int NT, typename T = float>
 __global__ void __launch_bounds__(256)
 rr_main_diag(const __grid_constant__ WalkArgs p) {
-    const float *x = (const float *)p.x;
+    const T *x = (const T *)p.x;
+    const u64 *lims = std::is_same<T, double>::value ? p.xkeys : p.keys;
     u32 c[NT];
 #pragma unroll
     for (int k = 0; k < NT; k++) c[k] = 0;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.nc;
          i += (long long)gridDim.x * blockDim.x) {
-        const float v = cell_dist_mem<float, NORM, EMB>(x + i, x + i, p.tau, p.emb);
+        const T v = cell_dist_mem<T, NORM, EMB>(x + i, x + i, p.tau, p.emb);
 #pragma unroll
-        for (int k = 0; k < NT; k++) c[k] += is_rec_lim(v, p.keys[k]) ? 1u : 0u;
+        for (int k = 0; k < NT; k++) c[k] += is_rec_lim(v, lims[k]) ? 1u : 0u;
     }
     const int lane = threadIdx.x & 31;
 #pragma unroll

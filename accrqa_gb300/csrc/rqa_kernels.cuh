@@ -1228,6 +1228,67 @@ det_diags(const __grid_constant__ WalkArgs p) {
 }
 
 // ---------------------------------------------------------------------------
+// RR of a float64 series through the float filter along diagonals, the DET
+// walk's lanes and units (lane q: diagonal 1 + 32 band + q, a unit one chunk of
+// a band's 32-cell blocks) with the float distance terms carried between
+// cells (compile-time tau TC): each block's filtered masks (ambiguous cells
+// decided again in float64) are counted instead of walked for runs.  The
+// strict upper triangle counts twice; the main diagonal is rr_main_diag's.
+// ---------------------------------------------------------------------------
+template <int NORM, int EMB, int NT, int TC>
+__global__ void __launch_bounds__(kWarpsPerCta * 32, kDiagMinCtas)
+rr_diag_tw_f64f(const __grid_constant__ WalkArgs p) {
+    __shared__ __align__(16) float stage_cta[kWarpsPerCta * DiagStage<F64F, 1>::kWords];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float *stage = stage_cta + warp * DiagStage<F64F, 1>::kWords;
+    const F64FPtr x = series_ptr<F64F>(p);
+    const long long gwarp = (long long)blockIdx.x * kWarpsPerCta + warp;
+    const long long nwarps = (long long)gridDim.x * kWarpsPerCta;
+    const long long nc = p.nc;
+    const long long tau = p.tau;
+    u64 total = 0;   // lane k: slot k
+    for (long long unit = gwarp; unit < p.nunits; unit += nwarps) {
+        const long long band = unit % p.nbands;
+        const long long nbk = p.nbands - band;
+        const long long kb = (unit / p.nbands) * p.chunk;
+        if (kb >= nbk) continue;   // warp-uniform
+        const long long ke = kb + p.chunk < nbk ? kb + p.chunk : nbk;
+        const long long d = 1 + band * 32 + lane;
+        const long long len = nc - d;
+        const long long wmin = nc - (band * 32 + 32);
+        long long s0 = kb * 32;
+        const long long se = ke * 32;
+        float tw[TermWindow<TC, EMB>::kN];
+        tw_begin_f64f<NORM, EMB, TC>(tw, x, s0, d);
+        u32 cnt[NT];
+#pragma unroll
+        for (int k = 0; k < NT; k++) cnt[k] = 0;
+        for (; s0 + 32 <= wmin && s0 < se; s0 += 32) {
+            u32 m[NT];
+            diag_masks_tw_f64f<NORM, EMB, NT, TC, false>(m, tw, x + s0, x + s0 + d, tau, 32,
+                                                         p.keys, p.xkeys, stage);
+#pragma unroll
+            for (int k = 0; k < NT; k++) cnt[k] += __popc(m[k]);
+        }
+        for (; s0 < se; s0 += 32) {
+            u32 m[NT];
+            diag_masks_tw_f64f<NORM, EMB, NT, TC, true>(m, tw, x + s0, x + s0 + d, tau, len - s0,
+                                                        p.keys, p.xkeys, stage);
+#pragma unroll
+            for (int k = 0; k < NT; k++) cnt[k] += __popc(m[k]);
+        }
+#pragma unroll
+        for (int k = 0; k < NT; k++) {
+            u32 t = cnt[k];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xFFFFFFFFu, t, o);
+            if (lane == k) total += 2ull * (u64)t;   // (i, j) and (j, i)
+        }
+    }
+    if (lane < p.nthr && lane < NT && total) atomicAdd(&p.counts[p.row[lane]], total);
+}
+
+// ---------------------------------------------------------------------------
 // LAM: lane r owns row i = 32*band + r of the full matrix and walks its
 // columns j = 0 .. nc-1 (chunked: one chunk of them), 32 at a time.
 // ---------------------------------------------------------------------------

@@ -28,6 +28,11 @@ void (*det_lt_term_window_kernel(int norm, int emb, int tau))(WalkArgs);
 void (*det_masks_term_window_kernel(int norm, int emb, int nt, int tau))(WalkArgs);
 // The same for float64 series through the float filter (walk_det_tw_f64f.cu).
 void (*det_f64f_term_window_kernel(int norm, int emb, int nt, int tau))(WalkArgs);
+// RR of float64 series through the filter along the DET walk's diagonals with
+// carried terms (rr_diag_tw_f64f; 4 or 8 thresholds, tau 1), and its
+// main-diagonal kernel; null when the shape has none (walk_det_tw_f64f.cu).
+void (*rr_f64f_term_window_kernel(int norm, int emb, int nt, int tau))(WalkArgs);
+void (*rr_f64_main_diag_kernel(int norm, int emb, int nt))(WalkArgs);
 
 // Filter limit pair of a padding slot: (-inf, -inf), surely not recurrent.
 constexpr u64 kNeverFilterPair = 0xFF800000FF800000ull;
@@ -309,6 +314,38 @@ static cudaError_t launch_rr_diag(const accrqa_walk_desc &d, cudaStream_t st) {
     return cudaGetLastError();
 }
 
+// RR of a float64 series through the filter along the DET walk's diagonals
+// (rr_diag_tw_f64f): the main diagonal exactly, then (band, chunk) units of
+// the strict upper triangle planned as the DET walk plans its (no records).
+static cudaError_t launch_rr_diag_tw_f64f(const accrqa_walk_desc &d, void (*kern)(WalkArgs),
+                                          void (*diag0)(WalkArgs), cudaStream_t st) {
+    WalkArgs a;
+    fill_walk_args<F64F>(d, a);
+    static std::atomic<int> c_tw{-1};
+    int per_sm = 0;
+    cudaError_t e = per_sm_of(kern, 0, c_tw, &per_sm);
+    if (e != cudaSuccess) return e;
+    const long long sms = sm_count_cached();
+    long long g0 = (d.nc + 255) / 256;
+    if (g0 > sms * 4) g0 = sms * 4;
+    if (g0 > 0 && diag0) {
+        diag0<<<(unsigned)g0, 256, 0, st>>>(a);
+        g_launches.fetch_add(1);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    if (d.nc < 2) return cudaSuccess;
+    const LinePlan q = plan_lines(true, d.nc, (int)sms, true,
+                                  accrqa_gb300_units_per_warp(ACCRQA_WALK_DET, d.nc));
+    a.nbands = q.nbands;
+    a.chunk = q.chunk;
+    // whole lines (one chunk) when the plan declines chunks: every band one unit
+    a.nunits = q.nrecords > 0 ? q.nunits : q.nbands;
+    if (q.nrecords == 0) a.chunk = q.nbands > 0 ? q.nbands : 1;
+    kern<<<grid_for(a.nunits, per_sm), kWarpsPerCta * 32, 0, st>>>(a);
+    g_launches.fetch_add(1);
+    return cudaGetLastError();
+}
+
 // RR of a float series with a fixed embedding along rows, counted by level
 // (16 slots with a bucket table; rr_rows' units).
 template <int NORM, int EMB>
@@ -330,6 +367,11 @@ static cudaError_t launch_rr_rows_levels(const WalkArgs &a0, cudaStream_t st) {
 template <int KIND, typename T, int NORM, int EMB, int NT>
 static cudaError_t launch_one(const accrqa_walk_desc &d, cudaStream_t st) {
     if constexpr (KIND == kWalkLevels) return launch_levels_one<T, NORM, EMB, NT>(d, st);
+    if constexpr (KIND == ACCRQA_WALK_RR && std::is_same<T, F64F>::value && EMB > 0 &&
+                  NT < kMaxThrPerPass) {
+        void (*tw)(WalkArgs) = rr_f64f_term_window_kernel(NORM, EMB, NT, d.tau);
+        if (tw) return launch_rr_diag_tw_f64f(d, tw, rr_f64_main_diag_kernel(NORM, EMB, NT), st);
+    }
     if constexpr (KIND == ACCRQA_WALK_RR && std::is_same<T, float>::value && EMB > 0) {
         if (rr_along_diagonals(EMB, d.tau, d.nthr, d.nc)) return launch_rr_diag<NORM, EMB, NT>(d, st);
         if constexpr (NT == kMaxThrPerPass) {

@@ -260,8 +260,12 @@ constexpr int kGroup = 8;
 // shift per cell moves its sign bit (recurrent) into the mask.  With STOP > 0
 // the warp checks every STOP-th slot whether any lane still has a recurrent
 // cell in the group and stops pushing when none has; the interval that
-// measured best differs per walker (LAM 4, RR 8, DET none).
-template <int NT, int STOP = 0>
+// measured best differs per walker (LAM 4, RR 8, DET none).  With AFTER1 the
+// warp also stops after slot 1 when no lane has pushed a recurrent cell of
+// the group there (one AND and one vote on the bits just pushed): the narrow
+// slots of a pass whose two widest limits are far apart -- white noise at
+// 0.1 .. 1.0 std -- are then mostly not evaluated at all.
+template <int NT, int STOP = 0, bool AFTER1 = false>
 __device__ __forceinline__ void push_group(u32 (&m)[NT], const f2 (&v)[kGroup / 2],
                                            const u64 (&keys)[kMaxThrPerPass]) {
     f2 d0[kGroup / 2];
@@ -304,11 +308,18 @@ __device__ __forceinline__ void push_group(u32 (&m)[NT], const f2 (&v)[kGroup / 
             m[k] = __funnelshift_l((u32)d[q], m[k], 1);
             m[k] = __funnelshift_l((u32)(d[q] >> 32), m[k], 1);
         }
+        if (AFTER1 && k == 1 && NT > 2 &&
+            !__any_sync(0xFFFFFFFFu, (m[1] & ((1u << kGroup) - 1u)) != 0u)) {
+#pragma unroll
+            for (int kk = 2; kk < NT; kk++) m[kk] <<= kGroup;
+            return;
+        }
     }
 }
 
-// double: an integer compare of the bit pattern against the limit.
-template <int NT, int STOP = 0>
+// double: an integer compare of the bit pattern against the limit (cell by
+// cell over all slots; AFTER1 has nothing to skip here).
+template <int NT, int STOP = 0, bool AFTER1 = false>
 __device__ __forceinline__ void push_group(u32 (&m)[NT], const double (&v)[kGroup],
                                            const u64 (&keys)[kMaxThrPerPass]) {
     u64 lo = (u64)__double_as_longlong(v[0]);

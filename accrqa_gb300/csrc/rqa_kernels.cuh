@@ -548,6 +548,65 @@ __device__ __forceinline__ u32 push_group_filtered(u32 (&m)[NT], const f2 (&v)[k
     return amb;
 }
 
+// Slot-major form of push_group_filtered, for the carried-term diagonal
+// walk: per slot, two f32x2 subtractions per cell pair (v - klo pushed into
+// the mask, v - khi for the ambiguity sign), the same operation count as the
+// cell-major form, so that the warp can stop after slot 1 when no lane has a
+// cell below khi_1 there.  khi does not grow from slot to slot (slots sorted
+// by decreasing exact limit, khi monotone in it), so such a group is surely
+// not recurrent and not ambiguous at every narrower slot: their masks shift
+// in zeros.  Same masks and ambiguous cells as push_group_filtered.
+template <int NT>
+__device__ __forceinline__ u32 push_group_filtered_sm(u32 (&m)[NT], const f2 (&v)[kGroup / 2],
+                                                      const u64 (&keys)[kMaxThrPerPass]) {
+    f2 dh0[kGroup / 2];
+    {
+        const float khi0 = __uint_as_float((u32)(keys[0] >> 32));
+        const f2 khi0x2 = pack2(khi0, khi0);
+        u64 any = 0;
+#pragma unroll
+        for (int q = 0; q < kGroup / 2; q++) {
+            dh0[q] = sub2(v[q], khi0x2);
+            any |= dh0[q];
+        }
+        if (!__any_sync(0xFFFFFFFFu, ((u32)any | (u32)(any >> 32)) >> 31)) {
+#pragma unroll
+            for (int k = 0; k < NT; k++) m[k] <<= kGroup;
+            return 0u;
+        }
+    }
+    u64 diff[kGroup / 2];   // sign bits: the cell is ambiguous at some slot
+#pragma unroll
+    for (int q = 0; q < kGroup / 2; q++) diff[q] = 0;
+#pragma unroll
+    for (int k = 0; k < NT; k++) {
+        const float klo = __uint_as_float((u32)keys[k]);
+        const float khi = __uint_as_float((u32)(keys[k] >> 32));
+        const f2 klo2 = pack2(klo, klo), khi2 = pack2(khi, khi);
+        u64 anyh = 0;
+#pragma unroll
+        for (int q = 0; q < kGroup / 2; q++) {
+            const f2 dl = sub2(v[q], klo2);
+            const f2 dh = k == 0 ? dh0[q] : sub2(v[q], khi2);
+            m[k] = __funnelshift_l((u32)dl, m[k], 1);
+            m[k] = __funnelshift_l((u32)(dl >> 32), m[k], 1);
+            diff[q] |= dl ^ dh;
+            if (k == 1) anyh |= dh;
+        }
+        if (k == 1 && NT > 2 &&
+            !__any_sync(0xFFFFFFFFu, ((u32)anyh | (u32)(anyh >> 32)) >> 31)) {
+#pragma unroll
+            for (int kk = 2; kk < NT; kk++) m[kk] <<= kGroup;
+            break;
+        }
+    }
+    u32 amb = 0;
+#pragma unroll
+    for (int q = 0; q < kGroup / 2; q++)
+        amb = (amb << 2) | (((u32)diff[q] >> 31) << 1) | (u32)(diff[q] >> 63);
+    return amb;
+}
+
 // Exact float64 decisions for the ambiguous cells of a group (rare): the
 // reference's distance in double, compared with the exact limits, written
 // over the cell's bit in every slot's mask.  xi/xj point at the cells'
@@ -689,7 +748,7 @@ __device__ __forceinline__ void diag_masks(u32 (&m)[NT], typename SeriesOf<T>::p
                 exact_fixup<NORM, EMB, NT>(m, amb, exact_ptr(xs) + g, 1, exact_ptr(xsd) + g, tau,
                                            emb, xkeys);
         } else {
-            push_group<NT>(m, v, keys);
+            push_group<NT, 0, true>(m, v, keys);
         }
     }
 }
@@ -709,7 +768,7 @@ __device__ __forceinline__ void diag_masks_tw(u32 (&m)[NT], float (&tw)[TermWind
     for (int g = 0; g < 32; g += kGroup) {
         f2 v[kGroup / 2];
         tw_group_values<NORM, EMB, TC, CHECK>(v, tw, stage, g, rem);
-        push_group<NT>(m, v, keys);
+        push_group<NT, 0, true>(m, v, keys);
     }
 }
 
@@ -795,7 +854,7 @@ __device__ __forceinline__ void diag_masks_tw_f64f(u32 (&m)[NT],
     for (int g = 0; g < 32; g += kGroup) {
         f2 v[kGroup / 2];
         tw_group_values_f64f<NORM, EMB, TC, CHECK>(v, tw, stage, g, rem);
-        const u32 amb = push_group_filtered<NT>(m, v, keys);
+        const u32 amb = push_group_filtered_sm<NT>(m, v, keys);
         if (__any_sync(0xFFFFFFFFu, amb != 0u))
             exact_fixup<NORM, EMB, NT>(m, amb, xs.d + g, 1, xsd.d + g, tau, EMB, xkeys);
     }

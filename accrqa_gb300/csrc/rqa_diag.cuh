@@ -37,8 +37,11 @@ namespace accrqa {
 // least 4 (the warp-wide skip decision covers 2 x GS cells per lane).
 template <int EMB> __host__ __device__ constexpr int rr_diag_group() { return EMB * ((4 + EMB - 1) / EMB); }
 
-// Resident CTAs per SM the diagonal RR walk is compiled for.
+// Resident CTAs per SM the diagonal RR walk is compiled for: slot masks 4
+// (5 and 6 measured 11% and 4% slower at N = 1e6, 4 thresholds), levels 6
+// (2% faster than 4 over the Lorenz N = 2e5 passes that take this walk).
 constexpr int kRrDiagMinCtas = 4;
+constexpr int kRrDiagLevelsMinCtas = 6;
 
 // The terms of one position t for the lane's two diagonals dA and dB:
 // tA = t + dA, tB = t + dB (indices below 2^31).
@@ -212,7 +215,7 @@ rr_main_diag(const __grid_constant__ WalkArgs p) {
 // LEVELS (16 slots): the cells are counted by level from the pass's bucket
 // table (rqa_level_table.cuh) instead of by slot masks.
 template <int NORM, int EMB, int NT, bool LEVELS = false>
-__global__ void __launch_bounds__(kWarpsPerCta * 32, kRrDiagMinCtas)
+__global__ void __launch_bounds__(kWarpsPerCta * 32, LEVELS ? kRrDiagLevelsMinCtas : kRrDiagMinCtas)
 rr_diags(const __grid_constant__ WalkArgs p) {
     constexpr int GS = rr_diag_group<EMB>();
     // masks: per-lane slot counters; levels: the table and per-lane level

@@ -279,6 +279,16 @@ template <int EMB> struct DiagStage<F64F, EMB> {
     static constexpr bool kOn = EMB > 0;
     static constexpr int kWords = EMB > 0 ? EMB * 192 : 1;
 };
+// The carried-term walks (TC > 0) stage one dimension: float as
+// diag_stage<1>; the float filter as diag_stage_f64f_tw -- A hi and lo (32
+// floats each), then the window's hi and lo pre-paired, (w[k], w[k+1]) for
+// k < 64, so that every operand pair of a cell pair is one 64-bit load.
+constexpr int kTwStageF64FWords = 64 + 4 * 64;
+template <typename T, int EMB, int TC> struct DetStage {
+    static constexpr int kWords = TC == 0 ? DiagStage<T, EMB>::kWords
+                                : std::is_same<T, F64F>::value ? kTwStageF64FWords
+                                                               : DiagStage<float, 1>::kWords;
+};
 
 template <int EMB>
 __device__ __forceinline__ void diag_stage(float *stage, const float *__restrict__ xs,
@@ -772,26 +782,47 @@ __device__ __forceinline__ void diag_masks_tw(u32 (&m)[NT], float (&tw)[TermWind
     }
 }
 
+// The one-dimension stage of the float filter's carried-term walk, positions
+// s0 + H + c (layout: DetStage).
+__device__ __forceinline__ void diag_stage_f64f_tw(float *stage, F64FPtr xs, F64FPtr xsd) {
+    const int lane = threadIdx.x & 31;
+    const int up = (lane + 1) & 31;
+    const float *wh = xsd.h - lane, *wl = xsd.l - lane;
+    f2 *bh = reinterpret_cast<f2 *>(stage + 64), *bl = reinterpret_cast<f2 *>(stage + 192);
+    __syncwarp();   // the previous block's reads are done
+    stage[lane] = __ldg(xs.h + lane);
+    stage[32 + lane] = __ldg(xs.l + lane);
+    const float h0 = __ldg(wh + lane), h1 = __ldg(wh + 32 + lane);
+    const float l0 = __ldg(wl + lane), l1 = __ldg(wl + 32 + lane);
+    const float th0 = __shfl_sync(0xFFFFFFFFu, h0, up), th1 = __shfl_sync(0xFFFFFFFFu, h1, up);
+    const float tl0 = __shfl_sync(0xFFFFFFFFu, l0, up), tl1 = __shfl_sync(0xFFFFFFFFu, l1, up);
+    bh[lane] = pack2(h0, lane < 31 ? th0 : th1);   // lane 31: (w[31], w[32])
+    bh[32 + lane] = pack2(h1, th1);                // k = 63 is never read
+    bl[lane] = pack2(l0, lane < 31 ? tl0 : tl1);
+    bl[32 + lane] = pack2(l1, tl1);
+    __syncwarp();
+}
+
 // float64 through the float filter, carried terms: the float term of a
 // position, ((h[t] - h[t+d]) + (l[t] - l[t+d]))^2, is exactly what the staged
 // filter evaluates for every cell and dimension that uses it, so the host's
-// bound holds; the stage is diag_stage_f64f<1> at positions s0 + H + c.
+// bound holds; the stage is diag_stage_f64f_tw at positions s0 + H + c.
 template <int NORM, int EMB, int TC, bool CHECK>
 __device__ __forceinline__ void tw_group_values_f64f(f2 (&v)[kGroup / 2],
                                                      float (&tw)[TermWindow<TC, EMB>::kN],
                                                      const float *stage, int g, long long rem) {
     constexpr int H = TermWindow<TC, EMB>::kH;
     const int lane = threadIdx.x & 31;
+    const f2 *bh = reinterpret_cast<const f2 *>(stage + 64);
+    const f2 *bl = reinterpret_cast<const f2 *>(stage + 192);
     float T[H + kGroup];
 #pragma unroll
     for (int m = 0; m < H; m++) T[m] = tw[m];
 #pragma unroll
     for (int q = 0; q < kGroup / 2; q++) {
         const int c = g + 2 * q, w = lane + c;
-        const f2 dh = sub2(*reinterpret_cast<const f2 *>(stage + c),
-                           pack2(stage[64 + w], stage[64 + w + 1]));
-        const f2 dl = sub2(*reinterpret_cast<const f2 *>(stage + 32 + c),
-                           pack2(stage[128 + w], stage[128 + w + 1]));
+        const f2 dh = sub2(*reinterpret_cast<const f2 *>(stage + c), bh[w]);
+        const f2 dl = sub2(*reinterpret_cast<const f2 *>(stage + 32 + c), bl[w]);
         const f2 dd = add2(dh, dl);
         const f2 e = NORM == kNormEuclidean ? mul2(dd, dd)
                                             : pack2(fabsf(lo_of(dd)), fabsf(hi_of(dd)));
@@ -849,7 +880,7 @@ __device__ __forceinline__ void diag_masks_tw_f64f(u32 (&m)[NT],
     constexpr int H = TermWindow<TC, EMB>::kH;
 #pragma unroll
     for (int k = 0; k < NT; k++) m[k] = 0;
-    diag_stage_f64f<1>(stage, xs + H, xsd + H, 1);
+    diag_stage_f64f_tw(stage, xs + H, xsd + H);
 #pragma unroll 1
     for (int g = 0; g < 32; g += kGroup) {
         f2 v[kGroup / 2];
@@ -1193,12 +1224,12 @@ template <typename T, int NORM, int EMB, int NT, int TC = 0>
 __global__ void __launch_bounds__(kWarpsPerCta * 32, kDiagMinCtas)
 det_diags(const __grid_constant__ WalkArgs p) {
     extern __shared__ u32 smem[];
-    __shared__ __align__(16) float stage_cta[kWarpsPerCta * DiagStage<T, EMB>::kWords];
+    __shared__ __align__(16) float stage_cta[kWarpsPerCta * DetStage<T, EMB, TC>::kWords];
     u32 *sh = smem;
     u32 *shmax = smem + NT * kShortRunBins;
     hist_smem_clear(sh, shmax, NT * kShortRunBins);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    float *stage = DiagStage<T, EMB>::kOn ? stage_cta + warp * DiagStage<T, EMB>::kWords : nullptr;
+    float *stage = DiagStage<T, EMB>::kOn ? stage_cta + warp * DetStage<T, EMB, TC>::kWords : nullptr;
     HistSink sink{sh, shmax, p.hist, p.hist_stride, p.row, nullptr};
     u32 carry[NT];
 
@@ -1297,9 +1328,9 @@ det_diags(const __grid_constant__ WalkArgs p) {
 template <int NORM, int EMB, int NT, int TC>
 __global__ void __launch_bounds__(kWarpsPerCta * 32, kDiagMinCtas)
 rr_diag_tw_f64f(const __grid_constant__ WalkArgs p) {
-    __shared__ __align__(16) float stage_cta[kWarpsPerCta * DiagStage<F64F, 1>::kWords];
+    __shared__ __align__(16) float stage_cta[kWarpsPerCta * kTwStageF64FWords];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    float *stage = stage_cta + warp * DiagStage<F64F, 1>::kWords;
+    float *stage = stage_cta + warp * kTwStageF64FWords;
     const F64FPtr x = series_ptr<F64F>(p);
     const long long gwarp = (long long)blockIdx.x * kWarpsPerCta + warp;
     const long long nwarps = (long long)gridDim.x * kWarpsPerCta;

@@ -332,14 +332,14 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, TC >= 4 ? kWideMinCtas : kD
 det_diags_lt(const __grid_constant__ WalkArgs p) {
     constexpr int NT = kMaxThrPerPass, NP = Planes<NT>::kN;
     extern __shared__ u32 smem[];
-    __shared__ __align__(16) float stage_cta[kWarpsPerCta * DiagStage<float, EMB>::kWords];
+    __shared__ __align__(16) float stage_cta[kWarpsPerCta * DetStage<float, EMB, TC>::kWords];
     __shared__ uint4 tbl[kLevelTableMax + 2];
     u32 *sh = smem;
     u32 *shmax = smem + NT * kShortRunBins;
     level_table_build(tbl, p);
     hist_smem_clear(sh, shmax, NT * kShortRunBins);   // (synchronizes the CTA)
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    float *stage = stage_cta + warp * DiagStage<float, EMB>::kWords;
+    float *stage = stage_cta + warp * DetStage<float, EMB, TC>::kWords;
     HistSink sink{sh, shmax, p.hist, p.hist_stride, p.row, nullptr};
     u32 carry[NT];
     const float *x = (const float *)p.x;

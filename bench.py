@@ -742,7 +742,11 @@ def roofline_1m_section(args, peak_f32, peak_f64):
 
 def run_case(args):
     """One pass of one kernel on a smaller series (for profiler captures):
-    --case rr|det|lam, --n samples, tau=1, emb=5, 16 thresholds.  --case batch
+    --case rr|det|lam, --n samples, tau=1, emb=5.  --series lorenz: the bench
+    series with its 16 thresholds; --series white|ar1: the N = 1e6 roofline
+    shapes (same generator, seed and standardisation) with thresholds
+    {0.1, 0.2, 0.5, 1.0} x std.  --dtype f64 goes through the host entry
+    points (float filter) instead of the device-resident ones.  --case batch
     runs the batched uneven workload (--batch-series series, RR+DET+LAM)
     warmup + steps times."""
     import torch
@@ -757,17 +761,35 @@ def run_case(args):
         print(json.dumps({"case": "batch", "series": len(jobs), "done": True}))
         return
     n = args.n
-    x = workloads.lorenz_x(n, SEED).astype(np.float32)
-    thr = (np.linspace(0.05, 0.8, NTHR) * float(np.std(x.astype(np.float64)))).astype(np.float32)
+    tau, emb = 1, 5
+    if args.series == "lorenz":
+        x = workloads.lorenz_x(n, SEED).astype(np.float32)
+        thr = (np.linspace(0.05, 0.8, NTHR) * float(np.std(x.astype(np.float64)))).astype(np.float32)
+    else:
+        gen = workloads.white if args.series == "white" else workloads.ar1
+        base = gen(n, SEED + 7)
+        base = (base - base.mean()) / base.std()
+        dt = np.float64 if args.dtype == "f64" else np.float32
+        x = base.astype(dt)
+        thr = (np.array([0.1, 0.2, 0.5, 1.0]) * float(np.std(x.astype(np.float64)))).astype(dt)
+        if args.dtype == "f64":
+            fn = {"rr": engine.rr_counts, "det": engine.det_histograms,
+                  "lam": engine.lam_histograms}[args.case]
+            for _ in range(args.warmup + args.steps):
+                fn(x, tau, emb, thr, 1)
+            torch.cuda.synchronize()
+            print(json.dumps({"case": args.case, "series": args.series, "dtype": "f64",
+                              "n": n, "done": True}))
+            return
+    nthr = len(thr)
     dev = torch.device("cuda", 0)
     sp = torch.cuda.current_stream(dev).cuda_stream
     dx = torch.zeros(n + 128, dtype=torch.float32, device=dev)
     dx[:n].copy_(torch.from_numpy(x))
-    tau, emb = 1, 5
     nc = n - (emb - 1) * tau
-    hist = torch.zeros(NTHR * (nc + 1), dtype=torch.int64, device=dev)
-    cnt = torch.zeros(NTHR, dtype=torch.int64, device=dev)
-    mx = torch.zeros(NTHR, dtype=torch.int32, device=dev)
+    hist = torch.zeros(nthr * (nc + 1), dtype=torch.int64, device=dev)
+    cnt = torch.zeros(nthr, dtype=torch.int64, device=dev)
+    mx = torch.zeros(nthr, dtype=torch.int32, device=dev)
     for _ in range(args.warmup + args.steps):
         hist.zero_()
         cnt.zero_()
@@ -781,7 +803,7 @@ def run_case(args):
             engine.lam_hist_dev(hist.data_ptr(), nc + 1, mx.data_ptr(), dx.data_ptr(),
                                 engine.F32, n, tau, emb, thr, 1, sp)
     torch.cuda.synchronize()
-    print(json.dumps({"case": args.case, "n": n, "done": True}))
+    print(json.dumps({"case": args.case, "series": args.series, "n": n, "done": True}))
 
 
 def main(argv=None):
@@ -789,6 +811,10 @@ def main(argv=None):
     ap.add_argument("--case", choices=["rr", "det", "lam", "batch"], default=None,
                     help="run a single pass of one kernel (profiling)")
     ap.add_argument("--n", type=int, default=50_000)
+    ap.add_argument("--series", choices=["lorenz", "white", "ar1"], default="lorenz",
+                    help="--case series (see run_case)")
+    ap.add_argument("--dtype", choices=["f32", "f64"], default="f32",
+                    help="--case series dtype (white/ar1 only)")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)

@@ -174,6 +174,15 @@ __device__ __forceinline__ f2 add2(f2 a, f2 b) {
     asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
     return r;
 }
+// The square of each half rounded once, RN(d * d), as a fused multiply-add
+// with +0: d * d is never -0, so adding +0 changes nothing, and a fused
+// result cannot be contracted further into a following addition (which a
+// packed multiply feeding a packed add can be).
+__device__ __forceinline__ f2 sq2(f2 d) {
+    f2 r;
+    asm("fma.rn.f32x2 %0, %1, %1, %2;" : "=l"(r) : "l"(d), "l"(0ull));
+    return r;
+}
 
 // ---------------------------------------------------------------------------
 // float64 series through a float filter.  Every sample x is split into

@@ -49,10 +49,7 @@ template <int NORM>
 __device__ __forceinline__ f2 diag_terms(const float *__restrict__ x, int t, int tA, int tB) {
     const float a = __ldg(x + t);
     const f2 d = sub2(pack2(a, a), pack2(__ldg(x + tA), __ldg(x + tB)));
-    if (NORM == kNormEuclidean)
-        // scalar squares: a packed square feeding the packed sums below could
-        // be contracted into a fused multiply-add by the code generator
-        return pack2(__fmul_rn(lo_of(d), lo_of(d)), __fmul_rn(hi_of(d), hi_of(d)));
+    if (NORM == kNormEuclidean) return sq2(d);   // not mul2: see sq2
     return pack2(fabsf(lo_of(d)), fabsf(hi_of(d)));
 }
 

@@ -340,8 +340,9 @@ __device__ __forceinline__ void tw_group_values(f2 (&v)[kGroup / 2],
         const int c = g + 2 * q;
         const f2 dd = sub2(*reinterpret_cast<const f2 *>(stage + c), stB[lane + c]);
         if (NORM == kNormEuclidean) {
-            T[H + 2 * q] = __fmul_rn(lo_of(dd), lo_of(dd));
-            T[H + 2 * q + 1] = __fmul_rn(hi_of(dd), hi_of(dd));
+            const f2 e = sq2(dd);
+            T[H + 2 * q] = lo_of(e);
+            T[H + 2 * q + 1] = hi_of(e);
         } else {
             T[H + 2 * q] = fabsf(lo_of(dd));
             T[H + 2 * q + 1] = fabsf(hi_of(dd));

@@ -225,28 +225,31 @@ __device__ __forceinline__ const T *exact_ptr(const T *x) { return x; }
 __device__ __forceinline__ const double *exact_ptr(F64FPtr x) { return x.d; }
 
 // Distances of two cells from their operand pairs a[m], b[m] (m = 0..emb-1).
-// Euclidean: difference and square on the f32x2 pipe, the running sum in the
-// reference's order with scalar adds.  The sum stays scalar on purpose: the
-// code generator contracts a packed multiply feeding a packed add into a
+// Euclidean: difference, square and running sum on the f32x2 pipe, each
+// rounded as the reference rounds it, the sum in its order m = 0..emb-1.  The
+// square is sq2 (a fused multiply-add with +0), not a packed multiply: the
+// code generator contracts a packed multiply feeding a packed add into one
 // fused multiply-add even when both carry .rn, which would round the square
 // and the sum once instead of twice (the oracle parity tests catch any such
 // change).  Maximal: the difference on the f32x2 pipe, |.| and the running
 // maximum per half.
 template <int NORM>
 struct Dist2 {
-    float al, ah;
+    float al, ah;   // maximal: the running maxima
+    f2 acc = 0;     // Euclidean: the running sums
     __device__ __forceinline__ void step(f2 a, f2 b, bool first) {
         const f2 d = sub2(a, b);
         if (NORM == kNormEuclidean) {
-            const f2 sq = mul2(d, d);
-            al = first ? lo_of(sq) : __fadd_rn(al, lo_of(sq));
-            ah = first ? hi_of(sq) : __fadd_rn(ah, hi_of(sq));
+            const f2 sq = sq2(d);
+            acc = first ? sq : add2(acc, sq);
         } else {
             al = fmaxf(first ? 0.0f : al, fabsf(lo_of(d)));
             ah = fmaxf(first ? 0.0f : ah, fabsf(hi_of(d)));
         }
     }
-    __device__ __forceinline__ f2 value() const { return pack2(al, ah); }
+    __device__ __forceinline__ f2 value() const {
+        return NORM == kNormEuclidean ? acc : pack2(al, ah);
+    }
 };
 
 // Value that is never recurrent (for cells past the end of a line).

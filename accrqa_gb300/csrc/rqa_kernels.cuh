@@ -353,7 +353,17 @@ __device__ __forceinline__ void tw_group_values(f2 (&v)[kGroup / 2],
 #pragma unroll
     for (int q = 0; q < kGroup / 2; q++) {
         float a0, a1;
-        if (NORM == kNormEuclidean) {
+        if (NORM == kNormEuclidean && TC % 2 == 0) {
+            // even tau: the terms of cells 2q and 2q+1 at dimension m are the
+            // two halves of one squared pair (new or carried), so the sums
+            // run on the f32x2 pipe, each half rounded as the scalar add
+            f2 acc = pack2(T[2 * q], T[2 * q + 1]);
+#pragma unroll
+            for (int m = 1; m < EMB; m++)
+                acc = add2(acc, pack2(T[2 * q + m * TC], T[2 * q + 1 + m * TC]));
+            a0 = lo_of(acc);
+            a1 = hi_of(acc);
+        } else if (NORM == kNormEuclidean) {
             a0 = T[2 * q];                      // 0 + e == e exactly
             a1 = T[2 * q + 1];
 #pragma unroll

@@ -26,8 +26,16 @@ namespace accrqa {
 
 constexpr int kLevelTableMax = 512;    // buckets of one table (8 KB of entries)
 
+// Level L (0..15 used) spread over the four bytes of a word, bit b of L at
+// bit 8b: the form in which levels_push8 gathers eight cells into planes.
+__host__ __device__ __forceinline__ u32 level_spread(u32 L) {
+    return ((L & 0xFu) * 0x00204081u) & 0x01010101u;
+}
+
 // Fields of WalkArgs used here: keys[] (float exclusive limits in the low
-// 32 bits, sorted), nthr, lt_shift, lt_lo, lt_nb.
+// 32 bits, sorted), nthr, lt_shift, lt_lo, lt_nb.  With SPREAD the entries
+// hold level_spread of the two levels instead of the levels themselves.
+template <bool SPREAD = false>
 __device__ __forceinline__ void level_table_build(uint4 *tbl, const WalkArgs &p) {
     const int n = p.lt_nb + 2;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
@@ -48,39 +56,43 @@ __device__ __forceinline__ void level_table_build(uint4 *tbl, const WalkArgs &p)
                 }
             }
         }
-        tbl[i] = make_uint4(bnd, lowc, lowc + mult, 0u);
+        tbl[i] = SPREAD ? make_uint4(bnd, level_spread(lowc), level_spread(lowc + mult), 0u)
+                        : make_uint4(bnd, lowc, lowc + mult, 0u);
     }
 }
 
-// Level of v (>= +0 or NaN).
+// Level of v (>= +0 or NaN).  The bucket index, clamped to [0, nb + 1], is
+// one fused add-min-max: max(min(b - base, nb + 1), 0).
 __device__ __forceinline__ u32 level_of(float v, const uint4 *tbl, int shift, int base, int nb) {
-    int d = (int)(__float_as_uint(v) >> shift) - base;
-    d = d < 0 ? 0 : (d > nb + 1 ? nb + 1 : d);
+    const int d = __viaddmin_s32_relu((int)(__float_as_uint(v) >> shift), -base, nb + 1);
     const uint4 e = tbl[d];
     return v < __uint_as_float(e.x) ? e.z : e.y;
 }
 
-// The levels of a group of 8 cells (v[q] = cells 2q, 2q+1) pushed into NP
-// bit planes, 8 bits each, the group's first cell highest: the levels are
-// packed one per byte, and for plane b the bytes' bit b is gathered into 8
-// adjacent bits by one multiplication -- (t0 << 4 | t1) * 0x08040201 puts
-// bit b of cell c at bit 31 - c, every other partial product below bit 24
-// or above bit 31, all at distinct positions (no carries).
+// The levels of a group of 8 cells (v[q] = cells 2q, 2q+1) pushed into the
+// five planes of levels 0..16, 8 bits each, the group's first cell highest.
+// The table holds spread levels (level_table_build<true>): cell c's word is
+// added at shift 7 - c, so byte b of the sum holds bit b of the 8 levels --
+// all at distinct positions, no carries -- and one byte permute appends it to
+// plane b (b < 4).  Plane 4, level 16, is the narrowest slot itself: the sign
+// of v - keys[15] (never set for a padding slot, whose limit is 0).
 template <int NP>
 __device__ __forceinline__ void levels_push8(u32 (&P)[NP], const f2 (&v)[4], const uint4 *tbl,
-                                             int shift, int base, int nb) {
-    u32 L[8];
+                                             int shift, int base, int nb, u64 key_last) {
+    static_assert(NP == 5, "16 slots: levels 0..16 in five planes");
+    u32 acc = 0;
 #pragma unroll
     for (int q = 0; q < 4; q++) {
-        L[2 * q] = level_of(lo_of(v[q]), tbl, shift, base, nb);
-        L[2 * q + 1] = level_of(hi_of(v[q]), tbl, shift, base, nb);
+        acc += level_of(lo_of(v[q]), tbl, shift, base, nb) << (7 - 2 * q);
+        acc += level_of(hi_of(v[q]), tbl, shift, base, nb) << (6 - 2 * q);
     }
-    const u32 w0 = L[0] | (L[1] << 8) | (L[2] << 16) | (L[3] << 24);
-    const u32 w1 = L[4] | (L[5] << 8) | (L[6] << 16) | (L[7] << 24);
 #pragma unroll
-    for (int b = 0; b < NP; b++) {
-        const u32 t0 = (w0 >> b) & 0x01010101u, t1 = (w1 >> b) & 0x01010101u;
-        P[b] = __funnelshift_l(((t0 << 4) | t1) * 0x08040201u, P[b], 8);
+    for (int b = 0; b < 4; b++) P[b] = __byte_perm(acc, P[b], 0x6540u + (u32)b);   // (P << 8) | byte b
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const f2 d = sub2(v[q], key_last);
+        P[4] = __funnelshift_l((u32)d, P[4], 1);
+        P[4] = __funnelshift_l((u32)(d >> 32), P[4], 1);
     }
 }
 

@@ -214,7 +214,7 @@ __device__ __forceinline__ void row_planes_levels(u32 (&P)[Planes<16>::kN],
             for (int b = 0; b < NP; b++) P[b] <<= kGroup;   // level 0 everywhere
             continue;
         }
-        levels_push8<NP>(P, v, tbl, shift, base, nb);
+        levels_push8<NP>(P, v, tbl, shift, base, nb, keys[kMaxThrPerPass - 1]);
     }
 }
 
@@ -224,7 +224,7 @@ tile_levels_lt(const __grid_constant__ WalkArgs p) {
     constexpr int NP = Planes<16>::kN;
     __shared__ __align__(16) float stage_cta[kWarpsPerCta * RowStage<float, EMB>::kWords];
     __shared__ uint4 tbl[kLevelTableMax + 2];
-    level_table_build(tbl, p);
+    level_table_build<true>(tbl, p);
     __syncthreads();
     float *stage = stage_cta + (threadIdx.x >> 5) * RowStage<float, EMB>::kWords;
     const float *x = (const float *)p.x;
@@ -293,7 +293,7 @@ __device__ __forceinline__ void diag_planes_levels(u32 (&P)[Planes<16>::kN],
             for (int b = 0; b < NP; b++) P[b] <<= kGroup;   // level 0 everywhere
             continue;
         }
-        levels_push8<NP>(P, v, tbl, shift, base, nb);
+        levels_push8<NP>(P, v, tbl, shift, base, nb, keys[kMaxThrPerPass - 1]);
     }
 }
 
@@ -321,7 +321,7 @@ __device__ __forceinline__ void diag_planes_levels_tw(u32 (&P)[Planes<16>::kN],
             for (int b = 0; b < NP; b++) P[b] <<= kGroup;   // level 0 everywhere
             continue;
         }
-        levels_push8<NP>(P, v, tbl, shift, base, nb);
+        levels_push8<NP>(P, v, tbl, shift, base, nb, keys[kMaxThrPerPass - 1]);
     }
 }
 
@@ -336,7 +336,7 @@ det_diags_lt(const __grid_constant__ WalkArgs p) {
     __shared__ uint4 tbl[kLevelTableMax + 2];
     u32 *sh = smem;
     u32 *shmax = smem + NT * kShortRunBins;
-    level_table_build(tbl, p);
+    level_table_build<true>(tbl, p);
     hist_smem_clear(sh, shmax, NT * kShortRunBins);   // (synchronizes the CTA)
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     float *stage = stage_cta + warp * DetStage<float, EMB, TC>::kWords;

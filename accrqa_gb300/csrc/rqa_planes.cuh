@@ -444,9 +444,14 @@ lam_levels(const __grid_constant__ WalkArgs p) {
             if (J > band) {
                 load_planes<NP>(P, p.planes, tile_index(band, J, T_));
             } else if (J < band) {
-                // row i left of the diagonal: column i of the tile (J, band)
+                // row i left of the diagonal: column i of the tile (J, band);
+                // a tile of level 0 everywhere (about a third of them on a
+                // chaotic series) is its own transpose
                 load_planes<NP>(P, p.planes, tile_index(J, band, T_));
-                warp_transpose<NP>(P);
+                u32 any = 0;
+#pragma unroll
+                for (int b = 0; b < NP; b++) any |= P[b];
+                if (__any_sync(0xFFFFFFFFu, any != 0u)) warp_transpose<NP>(P);
             } else {
                 u32 Q[NP];
                 load_planes<NP>(P, p.planes, tile_index(band, band, T_));

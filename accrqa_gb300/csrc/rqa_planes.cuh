@@ -325,10 +325,16 @@ __device__ __forceinline__ void diag_planes_levels_tw(u32 (&P)[Planes<16>::kN],
     }
 }
 
+// Resident CTAs per SM of det_diags_lt: a carried window of more than 32
+// terms (tau 8 at emb 6..8) needs the registers of 3 CTAs per SM.
+__host__ __device__ constexpr int det_lt_min_ctas(int tc, int emb) {
+    return tc * (emb - 1) > 32 ? 3 : (tc >= 4 ? kWideMinCtas : kDiagMinCtas);
+}
+
 // TC: 0 for any tau (operands staged per dimension), or the compile-time tau
 // of the carried-term walk.
 template <int NORM, int EMB, int TC = 0>
-__global__ void __launch_bounds__(kWarpsPerCta * 32, TC >= 4 ? kWideMinCtas : kDiagMinCtas)
+__global__ void __launch_bounds__(kWarpsPerCta * 32, det_lt_min_ctas(TC, EMB))
 det_diags_lt(const __grid_constant__ WalkArgs p) {
     constexpr int NT = kMaxThrPerPass, NP = Planes<NT>::kN;
     extern __shared__ u32 smem[];

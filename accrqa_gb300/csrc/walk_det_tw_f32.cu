@@ -1,7 +1,7 @@
 // Kernel instantiations of DET with the distance terms carried between cells
-// (float series): by levels (16 slots) for tau 1, 2, 4, and 8 up to emb 5 --
-// term windows (emb - 1) tau of at most 32 positions -- and by slot masks (4
-// or 8 slots) for tau 1; in a translation unit of their own so that they
+// (float series): by levels (16 slots) for tau 1, 2, 4 and 8 -- term windows
+// of (emb - 1) tau positions, up to 56 at 3 CTAs per SM -- and by slot masks
+// (4 or 8 slots) for tau 1; in a translation unit of their own so that they
 // compile beside the other DET kernels.
 #include "walk_dispatch.cuh"
 
@@ -13,9 +13,7 @@ static void (*tw_for_tau(int tau))(WalkArgs) {
         case 1: return det_diags_lt<NORM, EMB, 1>;
         case 2: return det_diags_lt<NORM, EMB, 2>;
         case 4: return det_diags_lt<NORM, EMB, 4>;
-        case 8:
-            if constexpr (EMB <= 5) return det_diags_lt<NORM, EMB, 8>;
-            return nullptr;
+        case 8: return det_diags_lt<NORM, EMB, 8>;
         default: return nullptr;
     }
 }

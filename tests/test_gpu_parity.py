@@ -21,8 +21,11 @@ def _cases():
     cases = []
     for dt in (np.float32, np.float64):
         for norm in NORMS:
+            # tau 8 at emb 3 and 6..8: the carried-term DET with term windows
+            # of 16 to 56 positions (the widest at 3 CTAs per SM)
             for (n, tau, emb) in [(97, 1, 1), (300, 1, 3), (451, 2, 5), (530, 3, 4),
-                                  (700, 1, 8), (256, 4, 2), (333, 7, 9), (129, 1, 2)]:
+                                  (700, 1, 8), (256, 4, 2), (333, 7, 9), (129, 1, 2),
+                                  (600, 8, 3), (900, 8, 6), (1100, 8, 7), (1200, 8, 8)]:
                 cases.append((dt, norm, n, tau, emb, int(rng.integers(0, 1 << 30))))
     return cases
 

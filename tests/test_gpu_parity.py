@@ -130,6 +130,37 @@ def test_edge_series(gpu, oracle_mod, dt):
                     lam[k], oracle_mod.lam_hist(x, 1, emb, t, norm), err_msg=f"{name} LAM {t}")
 
 
+def test_edge_series_by_levels(gpu, oracle_mod):
+    """The same special series through the float passes of more than 8
+    thresholds, which take their levels from the bucket table: NaN and inf
+    distances must come out at level 0 in the RR counts, the tile planes
+    (level 16 included) and the DET/LAM walks."""
+    specials = {
+        "nan_inf": np.array([0.1, np.nan, 0.3, np.inf, 0.2, -np.inf, 0.25, 0.26, 0.27,
+                             0.1, 0.3, 0.5] * 4),
+        "nan_signs": _nan_variety(np.float32),
+        "long_lines": np.tile(np.arange(10) / 10.0, 70),
+    }
+    thr = np.array([0.01, 0.02, 0.05, 0.08, 0.1, 0.15, 0.2, 0.3, 0.5, 0.7, 1.0, 2.0],
+                   dtype=np.float32)
+    for name, s in specials.items():
+        x = s.astype(np.float32)
+        for norm in NORMS:
+            for emb in (1, 2, 3):
+                rr = gpu.rr_counts(x, 1, emb, thr, norm)
+                np.testing.assert_array_equal(rr, oracle_mod.rr_counts(x, 1, emb, thr, norm),
+                                              err_msg=name)
+                det = gpu.det_histograms(x, 1, emb, thr, norm)
+                lam = gpu.lam_histograms(x, 1, emb, thr, norm)
+                for k, t in enumerate(thr):
+                    np.testing.assert_array_equal(
+                        det[k], oracle_mod.det_hist(x, 1, emb, t, norm),
+                        err_msg=f"{name} emb {emb} DET {t}")
+                    np.testing.assert_array_equal(
+                        lam[k], oracle_mod.lam_hist(x, 1, emb, t, norm),
+                        err_msg=f"{name} emb {emb} LAM {t}")
+
+
 @pytest.mark.parametrize("norm", NORMS)
 def test_rr_level_table_thresholds(gpu, oracle_mod, norm):
     """Float RR passes of more than 8 thresholds count cells by level from a

@@ -410,4 +410,33 @@ __device__ __forceinline__ void close_slot(u32 m, u32 &carry, int k, const Sink 
     }
 }
 
+// close_slot for two slots k and k + 1 of the same block, their dependent
+// chains interleaved (the same emits, in another order).
+template <class Sink>
+__device__ __forceinline__ void close_slot2(u32 m0, u32 m1, u32 &c0, u32 &c1, int k,
+                                            const Sink &sink) {
+    const bool f0 = m0 == 0xFFFFFFFFu, f1 = m1 == 0xFFFFFFFFu;
+    const u32 l0 = (u32)__clz(~m0), l1 = (u32)__clz(~m1);
+    const u32 a0 = c0 + l0, a1 = c1 + l1;
+    const u32 t0 = m0 & ~(m0 + 1u), t1 = m1 & ~(m1 + 1u);
+    u32 mid0 = m0 & ~t0 & __funnelshift_rc(0xFFFFFFFFu, 0u, l0);
+    u32 mid1 = m1 & ~t1 & __funnelshift_rc(0xFFFFFFFFu, 0u, l1);
+    c0 = f0 ? c0 + 32u : (u32)__popc(t0);
+    c1 = f1 ? c1 + 32u : (u32)__popc(t1);
+    if (!f0 && a0) sink.emit(k, a0);
+    if (!f1 && a1) sink.emit(k + 1, a1);
+    while (mid0) {
+        const u32 t = (u32)__clz(mid0);
+        const u32 len = (u32)__clz(~(mid0 << t));
+        sink.emit_short(k, len);
+        mid0 &= __funnelshift_rc(0xFFFFFFFFu, 0u, t + len);
+    }
+    while (mid1) {
+        const u32 t = (u32)__clz(mid1);
+        const u32 len = (u32)__clz(~(mid1 << t));
+        sink.emit_short(k + 1, len);
+        mid1 &= __funnelshift_rc(0xFFFFFFFFu, 0u, t + len);
+    }
+}
+
 }  // namespace accrqa

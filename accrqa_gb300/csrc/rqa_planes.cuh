@@ -124,11 +124,13 @@ __device__ __forceinline__ void load_planes(u32 (&P)[NP], const u32 *__restrict_
 template <int NT, int NP, class Sink>
 __device__ __forceinline__ void close_block_planes(const u32 (&P)[NP], u32 (&carry)[NT],
                                                    const Sink &sink) {
+    // two slots per step under one vote on the wider (slots nest: when no
+    // lane has a cell or an open run at slot k, none has at k + 1)
 #pragma unroll
-    for (int k = 0; k < NT; k++) {
-        const u32 m = mask_from_planes<NP>(P, k);
-        if (!__any_sync(0xFFFFFFFFu, (m | carry[k]) != 0u)) return;
-        close_slot(m, carry[k], k, sink);
+    for (int k = 0; k < NT; k += 2) {
+        const u32 m0 = mask_from_planes<NP>(P, k), m1 = mask_from_planes<NP>(P, k + 1);
+        if (!__any_sync(0xFFFFFFFFu, (m0 | carry[k]) != 0u)) return;
+        close_slot2(m0, m1, carry[k], carry[k + 1], k, sink);
     }
 }
 

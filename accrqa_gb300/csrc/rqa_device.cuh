@@ -410,32 +410,33 @@ __device__ __forceinline__ void close_slot(u32 m, u32 &carry, int k, const Sink 
     }
 }
 
-// close_slot for two slots k and k + 1 of the same block, their dependent
-// chains interleaved (the same emits, in another order).
-template <class Sink>
-__device__ __forceinline__ void close_slot2(u32 m0, u32 m1, u32 &c0, u32 &c1, int k,
-                                            const Sink &sink) {
-    const bool f0 = m0 == 0xFFFFFFFFu, f1 = m1 == 0xFFFFFFFFu;
-    const u32 l0 = (u32)__clz(~m0), l1 = (u32)__clz(~m1);
-    const u32 a0 = c0 + l0, a1 = c1 + l1;
-    const u32 t0 = m0 & ~(m0 + 1u), t1 = m1 & ~(m1 + 1u);
-    u32 mid0 = m0 & ~t0 & __funnelshift_rc(0xFFFFFFFFu, 0u, l0);
-    u32 mid1 = m1 & ~t1 & __funnelshift_rc(0xFFFFFFFFu, 0u, l1);
-    c0 = f0 ? c0 + 32u : (u32)__popc(t0);
-    c1 = f1 ? c1 + 32u : (u32)__popc(t1);
-    if (!f0 && a0) sink.emit(k, a0);
-    if (!f1 && a1) sink.emit(k + 1, a1);
-    while (mid0) {
-        const u32 t = (u32)__clz(mid0);
-        const u32 len = (u32)__clz(~(mid0 << t));
-        sink.emit_short(k, len);
-        mid0 &= __funnelshift_rc(0xFFFFFFFFu, 0u, t + len);
+// close_slot for W consecutive slots k .. k + W - 1 of the same block, their
+// dependent chains interleaved (the same emits, in another order); c points
+// at slot k's open-run length.
+template <int W, class Sink>
+__device__ __forceinline__ void close_slots(const u32 *m, u32 *c, int k, const Sink &sink) {
+    u32 a[W], mid[W];
+    bool f[W];
+#pragma unroll
+    for (int i = 0; i < W; i++) {
+        f[i] = m[i] == 0xFFFFFFFFu;
+        const u32 lead = (u32)__clz(~m[i]);
+        a[i] = c[i] + lead;
+        const u32 trail = m[i] & ~(m[i] + 1u);
+        mid[i] = m[i] & ~trail & __funnelshift_rc(0xFFFFFFFFu, 0u, lead);
+        c[i] = f[i] ? c[i] + 32u : (u32)__popc(trail);
     }
-    while (mid1) {
-        const u32 t = (u32)__clz(mid1);
-        const u32 len = (u32)__clz(~(mid1 << t));
-        sink.emit_short(k + 1, len);
-        mid1 &= __funnelshift_rc(0xFFFFFFFFu, 0u, t + len);
+#pragma unroll
+    for (int i = 0; i < W; i++)
+        if (!f[i] && a[i]) sink.emit(k + i, a[i]);
+#pragma unroll
+    for (int i = 0; i < W; i++) {
+        while (mid[i]) {
+            const u32 t = (u32)__clz(mid[i]);
+            const u32 len = (u32)__clz(~(mid[i] << t));
+            sink.emit_short(k + i, len);
+            mid[i] &= __funnelshift_rc(0xFFFFFFFFu, 0u, t + len);
+        }
     }
 }
 

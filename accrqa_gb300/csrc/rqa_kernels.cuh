@@ -944,6 +944,9 @@ __device__ __forceinline__ void runs_store(const u32 (&carry)[NT], u32 *trail) {
 // the widest threshold): a narrower slot's recurrent cells and open run lie
 // inside the wider slot's, so once no lane of the warp has either at slot k,
 // none has at the narrower slots and the warp stops.
+// (One vote per slot: the slot-mask walks serve passes of at most 8
+// thresholds, whose narrow slots are often empty; closing them in pairs
+// measured 256 -> 260 ms on white noise, 329 -> 324 ms on AR(1), N = 1e6.)
 template <int NT, class Sink>
 __device__ __forceinline__ void close_block(const u32 (&m)[NT], u32 (&carry)[NT],
                                             const Sink &sink) {

@@ -45,6 +45,10 @@ template <> struct Planes<4> { static constexpr int kN = 3; };
 template <> struct Planes<8> { static constexpr int kN = 4; };
 template <> struct Planes<16> { static constexpr int kN = 5; };
 
+// Slots the level walks close per step, their chains interleaved (a divisor
+// of the 16 slots).
+constexpr int kCloseWidth = 2;
+
 // Resident CTAs per SM of the plane walkers (they hold run state and a few
 // plane words, no operands).
 constexpr int kLevelMinCtas = 8;
@@ -124,13 +128,16 @@ __device__ __forceinline__ void load_planes(u32 (&P)[NP], const u32 *__restrict_
 template <int NT, int NP, class Sink>
 __device__ __forceinline__ void close_block_planes(const u32 (&P)[NP], u32 (&carry)[NT],
                                                    const Sink &sink) {
-    // two slots per step under one vote on the wider (slots nest: when no
-    // lane has a cell or an open run at slot k, none has at k + 1)
+    // kCloseWidth slots per step under one vote on the widest of them (slots
+    // nest: when no lane has a cell or an open run at slot k, none has at
+    // the narrower ones)
 #pragma unroll
-    for (int k = 0; k < NT; k += 2) {
-        const u32 m0 = mask_from_planes<NP>(P, k), m1 = mask_from_planes<NP>(P, k + 1);
-        if (!__any_sync(0xFFFFFFFFu, (m0 | carry[k]) != 0u)) return;
-        close_slot2(m0, m1, carry[k], carry[k + 1], k, sink);
+    for (int k = 0; k < NT; k += kCloseWidth) {
+        u32 m[kCloseWidth];
+#pragma unroll
+        for (int i = 0; i < kCloseWidth; i++) m[i] = mask_from_planes<NP>(P, k + i);
+        if (!__any_sync(0xFFFFFFFFu, (m[0] | carry[k]) != 0u)) return;
+        close_slots<kCloseWidth>(m, carry + k, k, sink);
     }
 }
 

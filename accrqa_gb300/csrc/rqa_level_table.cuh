@@ -26,8 +26,9 @@ namespace accrqa {
 
 constexpr int kLevelTableMax = 512;    // buckets of one table (8 KB of entries)
 
-// Level L (0..15 used) spread over the four bytes of a word, bit b of L at
-// bit 8b: the form in which levels_push8 gathers eight cells into planes.
+// The low four bits of level L spread over the four bytes of a word, bit b of
+// L at bit 8b: the form in which levels_push8 gathers eight cells into planes
+// 0-3 (level 16 spreads to 0; its plane 4 is decided apart).
 __host__ __device__ __forceinline__ u32 level_spread(u32 L) {
     return ((L & 0xFu) * 0x00204081u) & 0x01010101u;
 }

@@ -46,7 +46,7 @@ template <> struct Planes<8> { static constexpr int kN = 4; };
 template <> struct Planes<16> { static constexpr int kN = 5; };
 
 // Slots the level walks close per step, their chains interleaved (a divisor
-// of the 16 slots).
+// of their slot counts, 4, 8 and 16).
 constexpr int kCloseWidth = 2;
 
 // Resident CTAs per SM of the plane walkers (they hold run state and a few
